@@ -1,0 +1,145 @@
+/*
+ * jyulb_gb300.h -- C ABI of the GB300 D3Q19 isothermal lattice-Boltzmann
+ * engine (libjyulb_gb300.so).
+ *
+ * The reference exposes this path only as the Cython class
+ * jyulb.isothermal.Solver (jyulb/isothermal.pxd:38-114); it has no C ABI.
+ * Each entry point below replaces one step of that class's life cycle and
+ * cites it.  Conventions:
+ *   - plain pointers and sizes only; every host array uses the reference's
+ *     halo-padded C-order layout, (NI,NJ,NK) = (nx+2, ny+2, nz+2) with k
+ *     fastest, and (NI,NJ,NK,3) for vectors (jyulb/isothermal.pyx:234-248);
+ *   - functions return JLB_OK (0) or a negative status, never exit or trap;
+ *     jlb_last_error() gives the message for the last failure;
+ *   - a solver runs on one CUDA stream (its own unless one is supplied);
+ *     calls on one solver must not overlap (the same rule as the reference's
+ *     single Python object).
+ */
+#ifndef JYULB_GB300_H
+#define JYULB_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define JLB_OK 0
+#define JLB_ERR_INVALID_ARG (-1) /* ValueError in the reference          */
+#define JLB_ERR_STATE (-2)       /* RuntimeError in the reference        */
+#define JLB_ERR_CUDA (-3)        /* CUDA runtime failure                 */
+#define JLB_ERR_NOMEM (-4)       /* device or host allocation failure    */
+#define JLB_ERR_UNSUPPORTED (-5) /* valid request this build cannot run  */
+#define JLB_ERR_NUMERIC (-6)     /* NaN/Inf found by a reduction         */
+
+/* enumerations, values as in jyulb/defs.pxd:17-103 */
+#define JLB_BGK 0
+#define JLB_TRT 1
+#define JLB_REGULARIZATION 2
+#define JLB_WALL 0
+#define JLB_PERIODIC 1
+#define JLB_FIXED_DEN 2
+#define JLB_FIXED_VEL 3
+#define JLB_SYMMETRIC 4
+#define JLB_SOLID 0
+#define JLB_FLUID 1
+
+/* population storage / arithmetic of the time step */
+#define JLB_FP64 0 /* FP64 storage and arithmetic (parity path)          */
+#define JLB_FP32 1 /* FP32 storage of f_i - w_i, FP32 arithmetic          */
+#define JLB_FP16 2 /* FP16 storage of 2^12 (f_i/w_i - 1), FP32 arithmetic */
+
+typedef struct jlb_solver jlb_solver;
+
+typedef struct jlb_config {
+    int32_t lat_size[3]; /* interior lattice sites per axis (>= 1)          */
+    int32_t rlx_scheme;  /* JLB_BGK / JLB_TRT / JLB_REGULARIZATION           */
+    double kvisc;        /* kinematic viscosity, > 0                         */
+    double g[3];         /* uniform gravity                                  */
+    int32_t bc[6];       /* per face 1X,X1,1Y,Y1,1Z,Z1: JLB_WALL..SYMMETRIC  */
+    int32_t precision;   /* JLB_FP64 / JLB_FP32 / JLB_FP16                   */
+    double trt_magic;    /* TRT magic parameter; <= 0 selects the reference's
+                            fixed 8(2-w)/(8-w) odd rate (magic 3/16)         */
+    void *stream;        /* cudaStream_t to run on, or NULL                  */
+} jlb_config;
+
+/* Argument validation of Solver.__cinit__ / _check_bc
+ * (jyulb/isothermal.pyx:196-206, 378-426).  Writes the reference's message
+ * into msg (if not NULL) and returns JLB_ERR_INVALID_ARG on failure. */
+int jlb_check_config(const jlb_config *cfg, char *msg, size_t msg_len);
+
+/* Solver.__cinit__ (jyulb/isothermal.pyx:156-298): validate, derive the
+ * relaxation rates, allocate device state.  Needs a CUDA device. */
+int jlb_create(const jlb_config *cfg, jlb_solver **out);
+
+/* releases device state; NULL is ignored */
+void jlb_destroy(jlb_solver *s);
+
+/* Solver.finalize_init (jyulb/isothermal.pyx:1333-1365): applies the
+ * periodic/symmetric halo rules to phase, den and vel in place (as the
+ * reference does to its own arrays), classifies nodes, and sets the initial
+ * populations from den, vel and their finite-difference gradients
+ * (jyulb/isothermal.pyx:958-1105).  *nfluid receives the fluid-site count. */
+int jlb_finalize_init(jlb_solver *s, uint8_t *phase, double *den, double *vel,
+                      uint64_t *nfluid);
+
+/* Solver.evolve (jyulb/isothermal.pyx:1370-1418): re-reads the per-call
+ * inputs from the host arrays (Zou-He face data from the den/vel face layers,
+ * velocities of solid sites, den of sites next to moving solids, acc when
+ * acc != NULL), advances tsteps steps on the GPU, and writes the
+ * pre-collision density and velocity back into den and vel.  g is the
+ * gravity for this call (Solver.gravity).  *tot receives the total step
+ * count.  The halo layers of den/vel are refreshed from the boundary layers
+ * at the start of the call. */
+int jlb_evolve(jlb_solver *s, uint32_t tsteps, const double g[3], double *den,
+               double *vel, const double *acc, uint32_t *tot);
+
+/* Device-only stepping with the inputs of the last jlb_evolve call: no host
+ * synchronisation, no host arrays.  write_moments != 0 stores den/vel of the
+ * last step on the device (read them with jlb_download_moments). */
+int jlb_step(jlb_solver *s, uint32_t tsteps, int write_moments);
+
+/* copies the device den/vel of the last moment-writing step into the
+ * interior of the host arrays (layout as above) */
+int jlb_download_moments(jlb_solver *s, double *den, double *vel);
+
+/* Post-collision populations of the latest step as FP64, shape
+ * (19, nx, ny, nz) in the reference's lattice-vector order
+ * (jyulb/D3Q19.pxd:59-79); the reference keeps the same values in Solver.f1
+ * (Bundle-C order, jyulb/isothermal.pyx:1532-1704).  Solid sites read 0. */
+int jlb_get_populations(jlb_solver *s, double *f);
+
+/* overwrites the populations (same layout); used to restore a saved state */
+int jlb_set_populations(jlb_solver *s, const double *f);
+
+/* FP64 reductions over fluid sites of the last moment-writing step:
+ * out[0] = sum den, out[1..3] = sum den*u (stored u), out[4..6] = sum u,
+ * out[7] = number of non-finite den/u values found. */
+int jlb_reduce(jlb_solver *s, double out[8]);
+
+/* number of steps taken since finalize (Solver.tot_tsteps) */
+uint32_t jlb_tot_tsteps(const jlb_solver *s);
+
+/* relaxation rates (Solver.rlx_prm): out[0] = 1/tau_even, out[1] = 1/tau_odd */
+void jlb_rlx_prm(const jlb_solver *s, double out[2]);
+
+/* number of kernel launches issued by this solver so far */
+uint64_t jlb_kernel_launches(const jlb_solver *s);
+
+/* host<->device bytes moved by this solver so far: out[0] host to device,
+ * out[1] device to host (copies and in-place access to page-locked arrays) */
+void jlb_transfer_bytes(const jlb_solver *s, uint64_t out[2]);
+
+/* message of the last failure on s (or of the last failed jlb_create when s is
+ * NULL); never NULL */
+const char *jlb_last_error(const jlb_solver *s);
+
+/* static description of the build (architecture, kernels) */
+const char *jlb_build_info(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* JYULB_GB300_H */

@@ -1,0 +1,33 @@
+// lbm_aux.h -- host-callable launchers of the set-up / read-out / reduction
+// kernels (lbm_aux.cu).  All return a cudaError_t value.
+#pragma once
+#include <stdint.h>
+#include <cuda_runtime.h>
+
+namespace jlb {
+
+struct AuxGeom {
+    int nx, ny, nz;       // interior sizes
+    int NI, NJ, NK;       // halo-padded sizes of the host arrays
+    int64_t N, Np;        // interior node count, population slot stride
+};
+
+// initial populations from halo-padded phase/den/vel (device-accessible)
+int aux_init(int prec, const AuxGeom &g, const uint8_t *phase, const double *den, const double *vel, double w_e,
+             void *f, void *mden, void *mux, void *muy, void *muz, cudaStream_t st);
+// post-collision populations, FP64 (19, N); parity 0: post-collision slots,
+// 1: streamed slots
+int aux_readout(int prec, const AuxGeom &g, const void *f, const uint32_t *nmask, int parity, int M,
+                const int64_t *sp_node, const int64_t *sp_wr, double *out, cudaStream_t st);
+int aux_restore(int prec, const AuxGeom &g, void *f, const uint32_t *nmask, const double *in, cudaStream_t st);
+// moments of fluid nodes into device-accessible halo-padded host arrays
+int aux_download(int prec, const AuxGeom &g, const uint32_t *nmask, const void *den, const void *ux,
+                 const void *uy, const void *uz, double *hden, double *hvel, cudaStream_t st);
+// interior of a device-accessible halo-padded (NI,NJ,NK,3) array -> SoA field
+int aux_acc_upload(int prec, const AuxGeom &g, const double *hacc, void *acc, cudaStream_t st);
+int aux_reduce_blocks(int64_t N);
+// partial must hold 8 * nblocks doubles; out 8 doubles (device)
+int aux_reduce(int prec, const AuxGeom &g, const uint32_t *nmask, const void *den, const void *ux,
+               const void *uy, const void *uz, double *partial, int nblocks, double *out, cudaStream_t st);
+
+} // namespace jlb

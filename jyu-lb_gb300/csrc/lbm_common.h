@@ -1,0 +1,72 @@
+// lbm_common.h -- types shared by the host runtime and the CUDA kernels of
+// the D3Q19 engine.
+//
+// Lattice: the reference's D3Q19 enumeration (jyulb/D3Q19.pxd:59-79),
+//   q : 0(-1,-1,0) 1(-1,0,-1) 2(-1,0,0) 3(-1,0,1) 4(-1,1,0) 5(0,-1,-1)
+//       6(0,-1,0) 7(0,-1,1) 8(0,0,-1) 9(0,0,0) 10(0,0,1) 11(0,1,-1)
+//       12(0,1,0) 13(0,1,1) 14(1,-1,0) 15(1,0,-1) 16(1,0,0) 17(1,0,1) 18(1,1,0)
+// with opp(q) = 18 - q and weights w0 = 1/3 (q=9), w1 = 1/18 (one nonzero
+// component), w2 = 1/36 (two nonzero components).
+//
+// Device layout (one lattice, in place, AA pattern):
+//   f[q * Np + n], n = (i*ny + j)*nz + k over the interior nodes (no halo),
+//   Np = n_nodes rounded up to a multiple of 128.  Two step kinds alternate:
+//   "P" (pull-push) gathers f_q from A[opp(q)][x - c_q] and scatters f*_q to
+//   A[q][x + c_q]; "L" (local) reads A[q][x] and writes f*_q to A[opp(q)][x].
+//   Before a P step the array holds post-collision populations in reversed
+//   slots (A[opp(q)][x] = f*_q(x)); after it, the streamed populations
+//   (A[q][x] = incoming f_q(x)).
+#pragma once
+#include <stdint.h>
+#include <cuda_runtime.h>
+
+namespace jlb {
+
+constexpr int Q = 19;
+
+// node-mask bits (uint32 per node)
+constexpr uint32_t MASK_LINKS = 0x7FFFFu;      // bit q: link q bounces back
+constexpr uint32_t MASK_SPECIAL = 1u << 30;    // handled by the boundary-node path
+constexpr uint32_t MASK_SOLID = 1u << 31;      // not a fluid node
+constexpr uint32_t MASK_SKIP = MASK_SPECIAL | MASK_SOLID;
+
+// boundary-node info bits
+constexpr uint32_t SP_LADD_SHIFT = 0;  // bits 0..18: link has a moving-wall term
+constexpr uint32_t SP_FACE_SHIFT = 20; // bits 20..25: node lies on fixed face f
+
+enum Precision { PREC_FP64 = 0, PREC_FP32 = 1, PREC_FP16 = 2 };
+enum Scheme { SCH_BGK = 0, SCH_TRT = 1, SCH_REG = 2 };
+enum Bc { BC_WALL = 0, BC_PERIODIC = 1, BC_FIXED_DEN = 2, BC_FIXED_VEL = 3, BC_SYMMETRIC = 4 };
+
+struct StepArgs {
+    void *f;              // populations, 19 * Np elements of the storage type
+    int64_t Np;           // slot stride
+    int nx, ny, nz;
+    const uint32_t *nmask;
+    void *den, *ux, *uy, *uz; // moments (compute type); den holds rho-1 for shifted storage
+    const void *acc;      // optional acceleration field, 3 * Np (compute type), SoA
+    double g[3];          // uniform gravity
+    double w_e, w_o;      // relaxation rates 1/tau (even / odd)
+    int write_moments;
+    // dense-node grid
+    int bx, by, kblocks;  // block shape and k-blocks per row-block
+    int nb_dense;         // number of dense blocks; the rest are boundary blocks
+    // boundary (special) nodes
+    int M;                // number of boundary nodes
+    const int64_t *sp_node;
+    const uint32_t *sp_info;
+    const int64_t *sp_rd; // [19][M] P-step read element index
+    const int64_t *sp_wr; // [19][M] P-step write element index
+    const double *sp_lw;  // [19][M] c_q . u_wall of moving links
+    const double *sp_bc;  // [8][M] Zou-He data (den, ux, uy, uz) x 2 faces
+    void *sp_den;         // [M] previous-step density (compute type; rho-1 if shifted)
+    int bc[6];            // face kinds (for the Zou-He variant)
+};
+
+// launch entry points, one per precision translation unit
+// grid: `blocks` blocks of (a.bx, a.by) threads; returns a cudaError_t value
+int launch_step_fp64(const StepArgs &a, int scheme, bool pstep, bool accf, int blocks, cudaStream_t st);
+int launch_step_fp32(const StepArgs &a, int scheme, bool pstep, bool accf, int blocks, cudaStream_t st);
+int launch_step_fp16(const StepArgs &a, int scheme, bool pstep, bool accf, int blocks, cudaStream_t st);
+
+} // namespace jlb

@@ -1,0 +1,981 @@
+// lbm_host.cpp -- host runtime behind the C ABI (include/jyulb_gb300.h).
+//
+// Owns the device state of one D3Q19 solver, turns the reference's per-call
+// semantics (jyulb/isothermal.pyx:1370-1418) into device work, and keeps the
+// host-side bookkeeping the kernels need:
+//   * halo rules for phase/den/vel (periodic copy, symmetric mirror; x, y, z in
+//     the reference's order and index coverage, jyulb/isothermal.pyx:509-686);
+//   * the node mask (19 bounce-back bits per fluid node) and the boundary-node
+//     tables (Zou-He faces, symmetric-face links, moving solids);
+//   * the per-call inputs: Zou-He data from the den/vel face layers (with the
+//     reference's Z1 condition, jyulb/isothermal.pyx:500), solid velocities,
+//     previous-step density next to moving solids, acceleration field;
+//   * step sequencing of the AA pair, captured into CUDA graphs.
+#include <cuda_runtime.h>
+#include <omp.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "jyulb_gb300.h"
+#include "lbm_aux.h"
+#include "lbm_common.h"
+
+using namespace jlb;
+
+namespace {
+
+// lattice vectors (reference order)
+const int CI[19] = {-1, -1, -1, -1, -1, 0, 0, 0, 0, 0, 0, 0, 0, 0, 1, 1, 1, 1, 1};
+const int CJ[19] = {-1, 0, 0, 0, 1, -1, -1, -1, 0, 0, 0, 1, 1, 1, -1, 0, 0, 0, 1};
+const int CK[19] = {0, -1, 0, 1, 0, -1, 0, 1, -1, 0, 1, -1, 0, 1, 0, -1, 0, 1, 0};
+
+int find_q(int cx, int cy, int cz) {
+    for (int q = 0; q < 19; ++q)
+        if (CI[q] == cx && CJ[q] == cy && CK[q] == cz) return q;
+    return -1;
+}
+
+thread_local std::string g_create_error;
+
+struct DevBuf {
+    void *p = nullptr;
+    size_t bytes = 0;
+};
+
+} // namespace
+
+struct jlb_solver {
+    jlb_config cfg{};
+    int nx = 0, ny = 0, nz = 0, NI = 0, NJ = 0, NK = 0;
+    int64_t N = 0, Np = 0, NCNT = 0;
+    int prec = 0;
+    size_t ssz = 8, csz = 8;  // storage / compute element sizes
+    double we = 0, wo = 0;
+    AuxGeom geom{};
+    cudaStream_t st = nullptr;
+    bool own_stream = false;
+
+    // device state
+    void *f = nullptr;
+    uint32_t *nmask = nullptr;
+    void *mom[4] = {nullptr, nullptr, nullptr, nullptr};
+    void *acc = nullptr;
+    double *red_partial = nullptr, *red_out = nullptr;
+    int red_blocks = 0;
+    // boundary-node tables (device)
+    int M = 0, Mcap = 0;
+    int64_t *d_sp_node = nullptr, *d_sp_rd = nullptr, *d_sp_wr = nullptr;
+    uint32_t *d_sp_info = nullptr;
+    double *d_sp_lw = nullptr, *d_sp_bc = nullptr;
+    void *d_sp_den = nullptr;
+
+    // host bookkeeping
+    std::vector<uint8_t> phase;      // halo-padded snapshot after the halo rules
+    std::vector<uint32_t> hmask;     // Np entries
+    std::vector<int64_t> wall_pos;   // solid positions next to fluid (halo-padded index)
+    std::vector<double> wall_vel;    // their velocities at the last classification
+    std::vector<int64_t> sp_node;
+    std::vector<uint32_t> sp_info;
+    std::vector<int64_t> sp_rd, sp_wr;
+    std::vector<double> sp_lw, sp_bc;
+    std::vector<double> sp_den_h;
+    void *pinned = nullptr;          // staging for per-call uploads
+    size_t pinned_bytes = 0;
+
+    uint64_t nfluid = 0;
+    bool init_done = false;
+    uint32_t tot = 0;
+    int parity = 0;                  // 0: next step is P, 1: next step is L
+    bool accf = false;
+    double g[3] = {0, 0, 0};
+    uint64_t launches = 0;
+    uint64_t h2d_bytes = 0, d2h_bytes = 0; // host<->device traffic issued by the runtime
+    std::string err;
+
+    // graphs of GK consecutive steps without moment output, one per parity
+    cudaGraphExec_t gexec[2] = {nullptr, nullptr};
+    int GK = 32;
+    uint64_t args_version = 1, graph_version[2] = {0, 0};
+};
+
+namespace {
+
+int fail(jlb_solver *s, int code, const std::string &msg) {
+    if (s) s->err = msg;
+    else g_create_error = msg;
+    return code;
+}
+
+#define CK(call)                                                                                  \
+    do {                                                                                          \
+        cudaError_t e_ = (call);                                                                  \
+        if (e_ != cudaSuccess)                                                                    \
+            return fail(s, e_ == cudaErrorMemoryAllocation ? JLB_ERR_NOMEM : JLB_ERR_CUDA,        \
+                        std::string(#call) + ": " + cudaGetErrorString(e_));                      \
+    } while (0)
+
+#define CKR(expr)                                                                                 \
+    do {                                                                                          \
+        int r_ = (expr);                                                                          \
+        if (r_ != 0) return fail(s, JLB_ERR_CUDA, std::string(#expr) + ": " +                    \
+                                 cudaGetErrorString((cudaError_t)r_));                            \
+    } while (0)
+
+inline int64_t fidx(const jlb_solver *s, int I, int J, int K) {
+    return ((int64_t)I * s->NJ + J) * s->NK + K;
+}
+
+bool is_fixed(int b) { return b == BC_FIXED_DEN || b == BC_FIXED_VEL; }
+
+// face-plane iteration with the reference's coverage (x faces: interior j,k;
+// y faces: all i, interior k; z faces: all i, j)
+template <class F> void face_loop(const jlb_solver *s, int ax, F &&fn) {
+    int a0, A, b0, B;
+    if (ax == 0) { a0 = 1; A = s->NJ - 1; b0 = 1; B = s->NK - 1; }
+    else if (ax == 1) { a0 = 0; A = s->NI; b0 = 1; B = s->NK - 1; }
+    else { a0 = 0; A = s->NI; b0 = 0; B = s->NJ; }
+    for (int ua = a0; ua < A; ++ua)
+        for (int ub = b0; ub < B; ++ub) fn(ua, ub);
+}
+
+void plane(int ax, int c, int ua, int ub, int &I, int &J, int &K) {
+    if (ax == 0) { I = c; J = ua; K = ub; }
+    else if (ax == 1) { I = ua; J = c; K = ub; }
+    else { I = ua; J = ub; K = c; }
+}
+
+void halo_rw(const jlb_solver *s, int face, int &rd, int &wr) {
+    const int ax = face >> 1, side = face & 1;
+    const int n = ax == 0 ? s->NI : ax == 1 ? s->NJ : s->NK;
+    const bool per = s->cfg.bc[face] == BC_PERIODIC;
+    if (side == 0) { rd = 1; wr = per ? n - 1 : 0; }
+    else { rd = n - 2; wr = per ? 0 : n - 1; }
+}
+
+// jyulb/isothermal.pyx:509-577
+void enforce_phase(const jlb_solver *s, uint8_t *phase) {
+    for (int face = 0; face < 6; ++face) {
+        const int b = s->cfg.bc[face];
+        if (b != BC_PERIODIC && b != BC_SYMMETRIC) continue;
+        const int ax = face >> 1;
+        int rd, wr;
+        halo_rw(s, face, rd, wr);
+        face_loop(s, ax, [&](int ua, int ub) {
+            int I, J, K, I2, J2, K2;
+            plane(ax, rd, ua, ub, I, J, K);
+            plane(ax, wr, ua, ub, I2, J2, K2);
+            phase[fidx(s, I2, J2, K2)] = phase[fidx(s, I, J, K)];
+        });
+    }
+}
+
+// jyulb/isothermal.pyx:582-686
+void enforce_den_vel(const jlb_solver *s, double *den, double *vel) {
+    for (int face = 0; face < 6; ++face) {
+        const int b = s->cfg.bc[face];
+        if (b != BC_PERIODIC && b != BC_SYMMETRIC) continue;
+        const int ax = face >> 1;
+        int rd, wr;
+        halo_rw(s, face, rd, wr);
+        face_loop(s, ax, [&](int ua, int ub) {
+            int I, J, K, I2, J2, K2;
+            plane(ax, rd, ua, ub, I, J, K);
+            plane(ax, wr, ua, ub, I2, J2, K2);
+            const int64_t r = fidx(s, I, J, K), w = fidx(s, I2, J2, K2);
+            den[w] = den[r];
+            for (int d = 0; d < 3; ++d) {
+                const double v = vel[3 * r + d];
+                vel[3 * w + d] = (b == BC_SYMMETRIC && d == ax) ? -v : v;
+            }
+        });
+    }
+}
+
+// Halo positions outside a wall / Zou-He face are solid for the time step.
+// The reference leaves them SOLID unless a caller writes the halo directly;
+// forcing them keeps every fluid halo position mappable to an interior node.
+void solidify_closed_halo(const jlb_solver *s, std::vector<uint8_t> &phase) {
+    const int n[3] = {s->nx, s->ny, s->nz};
+#pragma omp parallel for schedule(static)
+    for (int I = 0; I < s->NI; ++I)
+        for (int J = 0; J < s->NJ; ++J)
+            for (int K = 0; K < s->NK; ++K) {
+                const int p[3] = {I - 1, J - 1, K - 1};
+                bool closed = false;
+                for (int ax = 0; ax < 3; ++ax) {
+                    if (p[ax] >= 0 && p[ax] < n[ax]) continue;
+                    const int b = s->cfg.bc[2 * ax + (p[ax] < 0 ? 0 : 1)];
+                    if (b != BC_PERIODIC && b != BC_SYMMETRIC) closed = true;
+                }
+                if (closed) phase[fidx(s, I, J, K)] = 0;
+            }
+}
+
+// c_q . u evaluated as the reference does (jyulb/isothermal.pyx:1122-1248):
+// sign of the first nonzero component times (u_a + u_b) or (u_a - u_b)
+double ladd_proj(int q, const double *u) {
+    const int c[3] = {CI[q], CJ[q], CK[q]};
+    int a = -1, b = -1;
+    for (int d = 0; d < 3; ++d)
+        if (c[d]) { if (a < 0) a = d; else b = d; }
+    double t;
+    if (b < 0) t = u[a];
+    else t = (c[a] == c[b]) ? (u[a] + u[b]) : (u[a] - u[b]);
+    return c[a] < 0 ? -t : t;
+}
+
+// Maps a halo-padded position that lies outside the interior through the
+// periodic / symmetric rules.  Returns the interior node index and updates q
+// to the mirrored direction; returns -1 if an axis has no such rule.
+int64_t map_halo(const jlb_solver *s, int I, int J, int K, int &q) {
+    int c[3] = {CI[q], CJ[q], CK[q]};
+    int p[3] = {I - 1, J - 1, K - 1};
+    const int n[3] = {s->nx, s->ny, s->nz};
+    for (int ax = 0; ax < 3; ++ax) {
+        if (p[ax] >= 0 && p[ax] < n[ax]) continue;
+        const bool low = p[ax] < 0;
+        const int b = s->cfg.bc[2 * ax + (low ? 0 : 1)];
+        if (b == BC_PERIODIC) p[ax] = low ? n[ax] - 1 : 0;
+        else if (b == BC_SYMMETRIC) { p[ax] = low ? 0 : n[ax] - 1; c[ax] = -c[ax]; }
+        else return -1;
+    }
+    q = find_q(c[0], c[1], c[2]);
+    return ((int64_t)p[0] * s->ny + p[1]) * s->nz + p[2];
+}
+
+int ensure_pinned(jlb_solver *s, size_t bytes) {
+    if (bytes <= s->pinned_bytes) return JLB_OK;
+    if (s->pinned) cudaFreeHost(s->pinned);
+    s->pinned = nullptr;
+    s->pinned_bytes = 0;
+    CK(cudaHostAlloc(&s->pinned, bytes, cudaHostAllocDefault));
+    s->pinned_bytes = bytes;
+    return JLB_OK;
+}
+
+// device address of a host array when the GPU can read/write it in place
+void *dev_view(const void *p) {
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged) return const_cast<void *>(p);
+    if (at.type == cudaMemoryTypeHost && at.devicePointer) return at.devicePointer;
+    return nullptr;
+}
+
+// ---------------------------------------------------------------------------
+// classification
+// ---------------------------------------------------------------------------
+void build_mask(jlb_solver *s) {
+    s->hmask.assign((size_t)s->Np, MASK_SOLID);
+    uint64_t cnt = 0;
+#pragma omp parallel for reduction(+ : cnt) schedule(static)
+    for (int i = 0; i < s->nx; ++i) {
+        for (int j = 0; j < s->ny; ++j)
+            for (int k = 0; k < s->nz; ++k) {
+                const int64_t n = ((int64_t)i * s->ny + j) * s->nz + k;
+                const int I = i + 1, J = j + 1, K = k + 1;
+                if (s->phase[fidx(s, I, J, K)] == 0) continue;
+                uint32_t m = 0;
+                for (int q = 0; q < 19; ++q) {
+                    if (q == 9) continue;
+                    if (s->phase[fidx(s, I - CI[q], J - CJ[q], K - CK[q])] == 0) m |= 1u << q;
+                }
+                s->hmask[n] = m;
+                ++cnt;
+            }
+    }
+    s->nfluid = cnt;
+}
+
+// solid positions that are the source of a bounce-back link
+void build_wall_list(jlb_solver *s) {
+    std::vector<uint8_t> flag((size_t)s->NCNT, 0);
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < s->nx; ++i)
+        for (int j = 0; j < s->ny; ++j)
+            for (int k = 0; k < s->nz; ++k) {
+                const int64_t n = ((int64_t)i * s->ny + j) * s->nz + k;
+                const uint32_t m = s->hmask[n];
+                if ((m & MASK_SOLID) || !(m & MASK_LINKS)) continue;
+                for (int q = 0; q < 19; ++q)
+                    if (m & (1u << q)) flag[fidx(s, i + 1 - CI[q], j + 1 - CJ[q], k + 1 - CK[q])] = 1;
+            }
+    s->wall_pos.clear();
+    for (int64_t p = 0; p < s->NCNT; ++p)
+        if (flag[p]) s->wall_pos.push_back(p);
+}
+
+// boundary-node tables from the current wall velocities (vel: halo-padded,
+// after the halo rules)
+void build_special(jlb_solver *s, const double *vel) {
+    const int64_t N = s->N;
+    std::vector<uint8_t> special((size_t)N, 0);
+    const int *bc = s->cfg.bc;
+    // Zou-He faces and symmetric faces: first / last interior layers
+    for (int face = 0; face < 6; ++face) {
+        const bool zh = is_fixed(bc[face]);
+        const bool sym = bc[face] == BC_SYMMETRIC;
+        if (!zh && !sym) continue;
+        const int ax = face >> 1;
+        const int lim = ax == 0 ? s->nx : ax == 1 ? s->ny : s->nz;
+        const int c = (face & 1) ? lim - 1 : 0;
+        const int A = ax == 0 ? s->ny : s->nx, B = ax == 2 ? s->ny : s->nz;
+        for (int a = 0; a < A; ++a)
+            for (int b2 = 0; b2 < B; ++b2) {
+                int i, j, k;
+                if (ax == 0) { i = c; j = a; k = b2; }
+                else if (ax == 1) { i = a; j = c; k = b2; }
+                else { i = a; j = b2; k = c; }
+                const int64_t n = ((int64_t)i * s->ny + j) * s->nz + k;
+                if (!(s->hmask[n] & MASK_SOLID)) special[n] = 1;
+            }
+    }
+    // moving solids: a bounce-back link with a nonzero Ladd projection
+    s->wall_vel.resize(3 * s->wall_pos.size());
+    for (size_t w = 0; w < s->wall_pos.size(); ++w) {
+        const int64_t p = s->wall_pos[w];
+        const double *u = vel + 3 * p;
+        s->wall_vel[3 * w] = u[0]; s->wall_vel[3 * w + 1] = u[1]; s->wall_vel[3 * w + 2] = u[2];
+        if (u[0] == 0.0 && u[1] == 0.0 && u[2] == 0.0) continue;
+        const int I = (int)(p / ((int64_t)s->NJ * s->NK));
+        const int J = (int)((p / s->NK) % s->NJ);
+        const int K = (int)(p % s->NK);
+        for (int q = 0; q < 19; ++q) {
+            if (q == 9) continue;
+            const int i = I + CI[q] - 1, j = J + CJ[q] - 1, k = K + CK[q] - 1;
+            if (i < 0 || j < 0 || k < 0 || i >= s->nx || j >= s->ny || k >= s->nz) continue;
+            const int64_t n = ((int64_t)i * s->ny + j) * s->nz + k;
+            if (s->hmask[n] & MASK_SOLID) continue;
+            if (ladd_proj(q, u) != 0.0) special[n] = 1;
+        }
+    }
+    // mark and build tables
+    for (int64_t n = 0; n < N; ++n) {
+        if (s->hmask[n] & MASK_SOLID) continue;
+        s->hmask[n] = special[n] ? (s->hmask[n] | MASK_SPECIAL) : (s->hmask[n] & ~MASK_SPECIAL);
+    }
+    s->sp_node.clear();
+    for (int64_t n = 0; n < N; ++n)
+        if (special[n]) s->sp_node.push_back(n);
+    const int M = (int)s->sp_node.size();
+    s->M = M;
+    s->sp_info.assign(M, 0);
+    s->sp_rd.assign((size_t)19 * M, 0);
+    s->sp_wr.assign((size_t)19 * M, 0);
+    s->sp_lw.assign((size_t)19 * M, 0.0);
+    s->sp_bc.assign((size_t)8 * M, 0.0);
+    s->sp_den_h.assign(M, 1.0);
+    const int64_t Np = s->Np;
+    for (int t = 0; t < M; ++t) {
+        const int64_t n = s->sp_node[t];
+        const int i = (int)(n / ((int64_t)s->ny * s->nz));
+        const int j = (int)((n / s->nz) % s->ny);
+        const int k = (int)(n % s->nz);
+        const int I = i + 1, J = j + 1, K = k + 1;
+        uint32_t info = 0;
+        for (int q = 0; q < 19; ++q) {
+            int64_t rd, wr;
+            if (q == 9) {
+                rd = wr = 9 * Np + n;
+            } else {
+                // read: source x - c_q
+                const int SI = I - CI[q], SJ = J - CJ[q], SK = K - CK[q];
+                const int64_t sp = fidx(s, SI, SJ, SK);
+                if (s->phase[sp] == 0) {
+                    rd = (int64_t)q * Np + n;
+                    const double lw = ladd_proj(q, vel + 3 * sp);
+                    if (lw != 0.0) {
+                        info |= 1u << q;
+                        s->sp_lw[(size_t)q * M + t] = lw;
+                    }
+                } else if (SI >= 1 && SI <= s->nx && SJ >= 1 && SJ <= s->ny && SK >= 1 && SK <= s->nz) {
+                    rd = (int64_t)(18 - q) * Np + (((int64_t)(SI - 1) * s->ny + (SJ - 1)) * s->nz + (SK - 1));
+                } else {
+                    int p = q;
+                    const int64_t m = map_halo(s, SI, SJ, SK, p);
+                    rd = m >= 0 ? (int64_t)(18 - p) * Np + m : (int64_t)q * Np + n;
+                }
+                // write: destination x + c_q
+                const int DI = I + CI[q], DJ = J + CJ[q], DK = K + CK[q];
+                const int64_t dp = fidx(s, DI, DJ, DK);
+                if (s->phase[dp] == 0) {
+                    wr = (int64_t)(18 - q) * Np + n;
+                } else if (DI >= 1 && DI <= s->nx && DJ >= 1 && DJ <= s->ny && DK >= 1 && DK <= s->nz) {
+                    wr = (int64_t)q * Np + (((int64_t)(DI - 1) * s->ny + (DJ - 1)) * s->nz + (DK - 1));
+                } else {
+                    int p = q;
+                    const int64_t m = map_halo(s, DI, DJ, DK, p);
+                    wr = m >= 0 ? (int64_t)p * Np + m : (int64_t)(18 - q) * Np + n;
+                }
+            }
+            s->sp_rd[(size_t)q * M + t] = rd;
+            s->sp_wr[(size_t)q * M + t] = wr;
+        }
+        // Zou-He faces of this node
+        const int at[6] = {i == 0, i == s->nx - 1, j == 0, j == s->ny - 1, k == 0, k == s->nz - 1};
+        for (int face = 0; face < 6; ++face)
+            if (at[face] && is_fixed(bc[face])) info |= 1u << (SP_FACE_SHIFT + face);
+        s->sp_info[t] = info;
+    }
+}
+
+// per-call Zou-He data and previous-step density of the boundary nodes
+void fill_dynamic(jlb_solver *s, const double *den, const double *vel) {
+    const int M = s->M;
+    const int *bc = s->cfg.bc;
+    for (int t = 0; t < M; ++t) {
+        const int64_t n = s->sp_node[t];
+        const int i = (int)(n / ((int64_t)s->ny * s->nz));
+        const int j = (int)((n / s->nz) % s->ny);
+        const int k = (int)(n % s->nz);
+        const int64_t fn = fidx(s, i + 1, j + 1, k + 1);
+        s->sp_den_h[t] = den[fn];
+        const uint32_t faces = (s->sp_info[t] >> SP_FACE_SHIFT) & 0x3Fu;
+        int slot = 0;
+        for (int face = 0; face < 6 && faces; ++face) {
+            if (!(faces & (1u << face))) continue;
+            // the reference refreshes face Z1's data when bc[Z1] is FIXED_DEN
+            // or bc[1Z] is FIXED_VEL (jyulb/isothermal.pyx:500); otherwise it
+            // keeps its initial den = 1, vel = 0
+            bool refresh = is_fixed(bc[face]);
+            if (face == 5) refresh = bc[5] == BC_FIXED_DEN || bc[4] == BC_FIXED_VEL;
+            double d = 1.0, u0 = 0.0, u1 = 0.0, u2 = 0.0;
+            if (refresh) { d = den[fn]; u0 = vel[3 * fn]; u1 = vel[3 * fn + 1]; u2 = vel[3 * fn + 2]; }
+            double *b = s->sp_bc.data();
+            b[(size_t)(4 * slot) * M + t] = d;
+            b[(size_t)(4 * slot + 1) * M + t] = u0;
+            b[(size_t)(4 * slot + 2) * M + t] = u1;
+            b[(size_t)(4 * slot + 3) * M + t] = u2;
+            slot = 1;
+        }
+    }
+}
+
+template <class T> int dev_alloc(jlb_solver *s, T *&p, size_t count) {
+    if (p) cudaFree(p);
+    p = nullptr;
+    if (count == 0) count = 1;
+    CK(cudaMalloc((void **)&p, count * sizeof(T)));
+    return JLB_OK;
+}
+
+void drop_graphs(jlb_solver *s) {
+    for (int p = 0; p < 2; ++p) {
+        if (s->gexec[p]) cudaGraphExecDestroy(s->gexec[p]);
+        s->gexec[p] = nullptr;
+        s->graph_version[p] = 0;
+    }
+}
+
+// uploads the static boundary tables (after build_special)
+int upload_tables(jlb_solver *s) {
+    const int M = s->M;
+    if (M > s->Mcap) {
+        const size_t cap = (size_t)M + M / 4 + 64;
+        int r;
+        if ((r = dev_alloc(s, s->d_sp_node, cap)) || (r = dev_alloc(s, s->d_sp_info, cap)) ||
+            (r = dev_alloc(s, s->d_sp_rd, 19 * cap)) || (r = dev_alloc(s, s->d_sp_wr, 19 * cap)) ||
+            (r = dev_alloc(s, s->d_sp_lw, 19 * cap)) || (r = dev_alloc(s, s->d_sp_bc, 8 * cap)))
+            return r;
+        if (s->d_sp_den) cudaFree(s->d_sp_den);
+        s->d_sp_den = nullptr;
+        CK(cudaMalloc(&s->d_sp_den, cap * s->csz));
+        s->Mcap = (int)cap;
+    }
+    if (M > 0) {
+        CK(cudaMemcpyAsync(s->d_sp_node, s->sp_node.data(), M * sizeof(int64_t), cudaMemcpyHostToDevice, s->st));
+        CK(cudaMemcpyAsync(s->d_sp_info, s->sp_info.data(), M * sizeof(uint32_t), cudaMemcpyHostToDevice, s->st));
+        CK(cudaMemcpyAsync(s->d_sp_rd, s->sp_rd.data(), 19 * (size_t)M * sizeof(int64_t), cudaMemcpyHostToDevice, s->st));
+        CK(cudaMemcpyAsync(s->d_sp_wr, s->sp_wr.data(), 19 * (size_t)M * sizeof(int64_t), cudaMemcpyHostToDevice, s->st));
+        CK(cudaMemcpyAsync(s->d_sp_lw, s->sp_lw.data(), 19 * (size_t)M * sizeof(double), cudaMemcpyHostToDevice, s->st));
+    }
+    CK(cudaMemcpyAsync(s->nmask, s->hmask.data(), (size_t)s->Np * sizeof(uint32_t), cudaMemcpyHostToDevice, s->st));
+    s->h2d_bytes += (uint64_t)s->Np * sizeof(uint32_t) + (uint64_t)M * (8 + 4 + 3 * 19 * 8);
+    CK(cudaStreamSynchronize(s->st)); // host vectors may be rebuilt right after
+    ++s->args_version;
+    return JLB_OK;
+}
+
+// uploads bc data and previous-step density of the boundary nodes
+int upload_dynamic(jlb_solver *s) {
+    const int M = s->M;
+    if (M == 0) return JLB_OK;
+    const size_t bc_bytes = 8 * (size_t)M * sizeof(double);
+    const size_t den_bytes = (size_t)M * s->csz;
+    int r = ensure_pinned(s, bc_bytes + den_bytes + 64);
+    if (r) return r;
+    CK(cudaStreamSynchronize(s->st)); // staging buffer may still be in flight
+    char *pin = (char *)s->pinned;
+    std::memcpy(pin, s->sp_bc.data(), bc_bytes);
+    char *dp = pin + bc_bytes;
+    if (s->prec == PREC_FP64) {
+        std::memcpy(dp, s->sp_den_h.data(), den_bytes);
+    } else {
+        float *fd = (float *)dp;
+        for (int t = 0; t < M; ++t) fd[t] = (float)(s->sp_den_h[t] - 1.0);
+    }
+    CK(cudaMemcpyAsync(s->d_sp_bc, pin, bc_bytes, cudaMemcpyHostToDevice, s->st));
+    s->h2d_bytes += bc_bytes + den_bytes;
+    CK(cudaMemcpyAsync(s->d_sp_den, dp, den_bytes, cudaMemcpyHostToDevice, s->st));
+    return JLB_OK;
+}
+
+StepArgs make_args(const jlb_solver *s, int write_moments) {
+    StepArgs a{};
+    a.f = s->f;
+    a.Np = s->Np;
+    a.nx = s->nx; a.ny = s->ny; a.nz = s->nz;
+    a.nmask = s->nmask;
+    a.den = s->mom[0]; a.ux = s->mom[1]; a.uy = s->mom[2]; a.uz = s->mom[3];
+    a.acc = s->accf ? s->acc : nullptr;
+    for (int d = 0; d < 3; ++d) a.g[d] = s->g[d];
+    a.w_e = s->we; a.w_o = s->wo;
+    a.write_moments = write_moments;
+    const int nzr = ((s->nz + 31) / 32) * 32;
+    a.bx = nzr >= 128 ? 128 : nzr;
+    a.by = 128 / a.bx;
+    a.kblocks = (s->nz + a.bx - 1) / a.bx;
+    const int64_t rows = (int64_t)s->nx * s->ny;
+    a.nb_dense = (int)(a.kblocks * ((rows + a.by - 1) / a.by));
+    a.M = s->M;
+    a.sp_node = s->d_sp_node; a.sp_info = s->d_sp_info;
+    a.sp_rd = s->d_sp_rd; a.sp_wr = s->d_sp_wr;
+    a.sp_lw = s->d_sp_lw; a.sp_bc = s->d_sp_bc;
+    a.sp_den = s->d_sp_den;
+    for (int f = 0; f < 6; ++f) a.bc[f] = s->cfg.bc[f];
+    return a;
+}
+
+int launch_one(jlb_solver *s, const StepArgs &a, bool pstep) {
+    const int blocks = a.nb_dense + (a.M + 127) / 128;
+    int r;
+    if (s->prec == PREC_FP64) r = launch_step_fp64(a, s->cfg.rlx_scheme, pstep, s->accf, blocks, s->st);
+    else if (s->prec == PREC_FP32) r = launch_step_fp32(a, s->cfg.rlx_scheme, pstep, s->accf, blocks, s->st);
+    else r = launch_step_fp16(a, s->cfg.rlx_scheme, pstep, s->accf, blocks, s->st);
+    if (r) return fail(s, JLB_ERR_CUDA, std::string("step launch: ") + cudaGetErrorString((cudaError_t)r));
+    ++s->launches;
+    return JLB_OK;
+}
+
+bool graphs_enabled() {
+    static int en = -1;
+    if (en < 0) {
+        const char *e = std::getenv("JLB_NO_GRAPH");
+        en = (e && e[0] && e[0] != '0') ? 0 : 1;
+    }
+    return en == 1;
+}
+
+// runs n steps; the last one writes moments when write_last
+int run_steps(jlb_solver *s, uint32_t n, bool write_last) {
+    if (n == 0) return JLB_OK;
+    const StepArgs a0 = make_args(s, 0);
+    uint32_t plain = write_last ? n - 1 : n;
+    if (graphs_enabled() && plain >= (uint32_t)s->GK) {
+        while (plain >= (uint32_t)s->GK) {
+            const int p = s->parity;
+            if (!s->gexec[p] || s->graph_version[p] != s->args_version) {
+                if (s->gexec[p]) cudaGraphExecDestroy(s->gexec[p]);
+                s->gexec[p] = nullptr;
+                cudaGraph_t graph;
+                CK(cudaStreamBeginCapture(s->st, cudaStreamCaptureModeThreadLocal));
+                int par = p;
+                int rr = JLB_OK;
+                for (int t = 0; t < s->GK && rr == JLB_OK; ++t) {
+                    rr = launch_one(s, a0, par == 0);
+                    par ^= 1;
+                }
+                cudaError_t ce = cudaStreamEndCapture(s->st, &graph);
+                if (rr) return rr;
+                if (ce != cudaSuccess) return fail(s, JLB_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ce));
+                s->launches -= s->GK; // capture does not launch
+                ce = cudaGraphInstantiate(&s->gexec[p], graph, 0);
+                cudaGraphDestroy(graph);
+                if (ce != cudaSuccess) return fail(s, JLB_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ce));
+                s->graph_version[p] = s->args_version;
+            }
+            CK(cudaGraphLaunch(s->gexec[p], s->st));
+            s->launches += s->GK;
+            plain -= s->GK;
+            if (s->GK & 1) s->parity ^= 1;
+        }
+    }
+    for (uint32_t t = 0; t < plain; ++t) {
+        int r = launch_one(s, a0, s->parity == 0);
+        if (r) return r;
+        s->parity ^= 1;
+    }
+    if (write_last) {
+        const StepArgs a1 = make_args(s, 1);
+        int r = launch_one(s, a1, s->parity == 0);
+        if (r) return r;
+        s->parity ^= 1;
+    }
+    return JLB_OK;
+}
+
+int download(jlb_solver *s, double *den, double *vel) {
+    const size_t nb = (size_t)s->NCNT * sizeof(double);
+    double *dd = (double *)dev_view(den);
+    double *dv = (double *)dev_view(vel);
+    if (dd && dv) {
+        CKR(aux_download(s->prec, s->geom, s->nmask, s->mom[0], s->mom[1], s->mom[2], s->mom[3], dd, dv, s->st));
+        s->d2h_bytes += s->nfluid * 4 * sizeof(double);
+        ++s->launches;
+        CK(cudaStreamSynchronize(s->st));
+        return JLB_OK;
+    }
+    // host arrays the GPU cannot address: round trip through device copies
+    double *tden = nullptr, *tvel = nullptr;
+    CK(cudaMalloc(&tden, nb));
+    cudaError_t e = cudaMalloc(&tvel, 3 * nb);
+    if (e != cudaSuccess) { cudaFree(tden); return fail(s, JLB_ERR_NOMEM, "download staging allocation"); }
+    int r = JLB_OK;
+    if (cudaMemcpyAsync(tden, den, nb, cudaMemcpyHostToDevice, s->st) != cudaSuccess ||
+        cudaMemcpyAsync(tvel, vel, 3 * nb, cudaMemcpyHostToDevice, s->st) != cudaSuccess ||
+        aux_download(s->prec, s->geom, s->nmask, s->mom[0], s->mom[1], s->mom[2], s->mom[3], tden, tvel, s->st) ||
+        cudaMemcpyAsync(den, tden, nb, cudaMemcpyDeviceToHost, s->st) != cudaSuccess ||
+        cudaMemcpyAsync(vel, tvel, 3 * nb, cudaMemcpyDeviceToHost, s->st) != cudaSuccess ||
+        cudaStreamSynchronize(s->st) != cudaSuccess)
+        r = fail(s, JLB_ERR_CUDA, std::string("staged download: ") + cudaGetErrorString(cudaGetLastError()));
+    ++s->launches;
+    cudaFree(tden);
+    cudaFree(tvel);
+    return r;
+}
+
+} // namespace
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+extern "C" {
+
+int jlb_check_config(const jlb_config *cfg, char *msg, size_t msg_len) {
+    auto bad = [&](const char *m) {
+        if (msg && msg_len) { std::snprintf(msg, msg_len, "%s", m); }
+        return JLB_ERR_INVALID_ARG;
+    };
+    if (!cfg) return bad("Invalid configuration (NULL).");
+    if (cfg->lat_size[0] < 1 || cfg->lat_size[1] < 1 || cfg->lat_size[2] < 1)
+        return bad("Invalid lattice size input.");
+    if (cfg->rlx_scheme != JLB_BGK && cfg->rlx_scheme != JLB_TRT && cfg->rlx_scheme != JLB_REGULARIZATION)
+        return bad("Invalid relaxation scheme input.");
+    if (!(cfg->kvisc > 0.0)) return bad("Invalid kinematic viscosity input.");
+    const int32_t *bc = cfg->bc;
+    for (int f = 0; f < 6; ++f)
+        if (bc[f] < JLB_WALL || bc[f] > JLB_SYMMETRIC) return bad("Invalid boundary condition input.");
+    const char *dirs[3] = {"Invalid periodic bc setup (in x-dir.).", "Invalid periodic bc setup (in y-dir.).",
+                           "Invalid periodic bc setup (in z-dir.)."};
+    for (int ax = 0; ax < 3; ++ax) {
+        const int a = bc[2 * ax], b = bc[2 * ax + 1];
+        if ((a == JLB_PERIODIC || b == JLB_PERIODIC) && a != b) return bad(dirs[ax]);
+    }
+    bool fx[3];
+    for (int ax = 0; ax < 3; ++ax) fx[ax] = is_fixed(bc[2 * ax]) || is_fixed(bc[2 * ax + 1]);
+    if ((fx[0] && (fx[1] || fx[2])) || (fx[1] && (fx[0] || fx[2])) || (fx[2] && (fx[0] || fx[1])))
+        return bad("Invalid fixed variable bc setup.");
+    if (cfg->precision < JLB_FP64 || cfg->precision > JLB_FP16) return bad("Invalid precision input.");
+    if (std::isnan(cfg->trt_magic)) return bad("Invalid TRT magic parameter input.");
+    for (int d = 0; d < 3; ++d)
+        if (!std::isfinite(cfg->g[d])) return bad("Invalid gravity input.");
+    return JLB_OK;
+}
+
+int jlb_create(const jlb_config *cfg, jlb_solver **out) {
+    jlb_solver *s = nullptr;
+    if (!out) return fail(nullptr, JLB_ERR_INVALID_ARG, "out is NULL");
+    *out = nullptr;
+    char msg[256];
+    if (jlb_check_config(cfg, msg, sizeof msg) != JLB_OK) return fail(nullptr, JLB_ERR_INVALID_ARG, msg);
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
+        cudaGetLastError();
+        return fail(nullptr, JLB_ERR_CUDA, "no CUDA device available");
+    }
+    s = new jlb_solver();
+    s->cfg = *cfg;
+    s->nx = cfg->lat_size[0]; s->ny = cfg->lat_size[1]; s->nz = cfg->lat_size[2];
+    s->NI = s->nx + 2; s->NJ = s->ny + 2; s->NK = s->nz + 2;
+    s->N = (int64_t)s->nx * s->ny * s->nz;
+    s->Np = ((s->N + 127) / 128) * 128;
+    s->NCNT = (int64_t)s->NI * s->NJ * s->NK;
+    s->prec = cfg->precision;
+    s->ssz = s->prec == PREC_FP64 ? 8 : s->prec == PREC_FP32 ? 4 : 2;
+    s->csz = s->prec == PREC_FP64 ? 8 : 4;
+    for (int d = 0; d < 3; ++d) s->g[d] = cfg->g[d];
+    // relaxation rates (jyulb/isothermal.pyx:274-287)
+    const double tau_e = 0.5 + 3.0 * cfg->kvisc;
+    s->we = 1.0 / tau_e;
+    if (cfg->rlx_scheme == JLB_TRT) {
+        if (cfg->trt_magic > 0.0) s->wo = 1.0 / (cfg->trt_magic / (tau_e - 0.5) + 0.5);
+        else s->wo = 8.0 * (2.0 - s->we) / (8.0 - s->we);
+    }
+    s->geom = AuxGeom{s->nx, s->ny, s->nz, s->NI, s->NJ, s->NK, s->N, s->Np};
+    int r = JLB_OK;
+    auto bail = [&](int code) {
+        std::string m = s->err;
+        jlb_destroy(s);
+        fail(nullptr, code, m);
+        return code;
+    };
+    if (cfg->stream) {
+        s->st = (cudaStream_t)cfg->stream;
+    } else {
+        if (cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking) != cudaSuccess) {
+            s->err = "cudaStreamCreate failed";
+            return bail(JLB_ERR_CUDA);
+        }
+        s->own_stream = true;
+    }
+    auto alloc = [&](void **p, size_t bytes) {
+        cudaError_t e = cudaMalloc(p, bytes);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            s->err = std::string("device allocation of ") + std::to_string(bytes) + " bytes failed: " +
+                     cudaGetErrorString(e);
+            return JLB_ERR_NOMEM;
+        }
+        return JLB_OK;
+    };
+    if ((r = alloc(&s->f, (size_t)19 * s->Np * s->ssz))) return bail(r);
+    if ((r = alloc((void **)&s->nmask, (size_t)s->Np * sizeof(uint32_t)))) return bail(r);
+    for (int c = 0; c < 4; ++c)
+        if ((r = alloc(&s->mom[c], (size_t)s->Np * s->csz))) return bail(r);
+    s->red_blocks = aux_reduce_blocks(s->N);
+    if ((r = alloc((void **)&s->red_partial, (size_t)8 * s->red_blocks * sizeof(double)))) return bail(r);
+    if ((r = alloc((void **)&s->red_out, 8 * sizeof(double)))) return bail(r);
+    *out = s;
+    return JLB_OK;
+}
+
+void jlb_destroy(jlb_solver *s) {
+    if (!s) return;
+    if (s->st) cudaStreamSynchronize(s->st);
+    drop_graphs(s);
+    void *bufs[] = {s->f, s->nmask, s->mom[0], s->mom[1], s->mom[2], s->mom[3], s->acc, s->red_partial,
+                    s->red_out, s->d_sp_node, s->d_sp_info, s->d_sp_rd, s->d_sp_wr, s->d_sp_lw, s->d_sp_bc,
+                    s->d_sp_den};
+    for (void *p : bufs)
+        if (p) cudaFree(p);
+    if (s->pinned) cudaFreeHost(s->pinned);
+    if (s->own_stream && s->st) cudaStreamDestroy(s->st);
+    delete s;
+}
+
+int jlb_finalize_init(jlb_solver *s, uint8_t *phase, double *den, double *vel, uint64_t *nfluid) {
+    if (!s || !phase || !den || !vel) return fail(s, JLB_ERR_INVALID_ARG, "NULL argument");
+    // fluid sites of the interior (jyulb/isothermal.pyx:1354-1356)
+    uint64_t cnt = 0;
+    for (int I = 1; I < s->NI - 1; ++I)
+        for (int J = 1; J < s->NJ - 1; ++J)
+            for (int K = 1; K < s->NK - 1; ++K) cnt += phase[fidx(s, I, J, K)] != 0;
+    drop_graphs(s);
+    s->M = 0;
+    if (cnt >= 1) {
+        enforce_phase(s, phase);
+        enforce_den_vel(s, den, vel);
+        s->phase.assign(phase, phase + s->NCNT);
+        solidify_closed_halo(s, s->phase);
+        build_mask(s);
+        build_wall_list(s);
+        build_special(s, vel);
+        int r = upload_tables(s);
+        if (r) return r;
+        // initial populations: the kernel reads the halo-padded arrays
+        const size_t nb = (size_t)s->NCNT;
+        uint8_t *dph = nullptr;
+        double *dden = nullptr, *dvel = nullptr;
+        CK(cudaMalloc(&dph, nb));
+        cudaError_t e1 = cudaMalloc(&dden, nb * sizeof(double));
+        cudaError_t e2 = cudaMalloc(&dvel, 3 * nb * sizeof(double));
+        if (e1 != cudaSuccess || e2 != cudaSuccess) {
+            cudaFree(dph); cudaFree(dden); cudaFree(dvel);
+            return fail(s, JLB_ERR_NOMEM, "initialisation staging allocation");
+        }
+        CK(cudaMemcpyAsync(dph, phase, nb, cudaMemcpyHostToDevice, s->st));
+        CK(cudaMemcpyAsync(dden, den, nb * sizeof(double), cudaMemcpyHostToDevice, s->st));
+        CK(cudaMemcpyAsync(dvel, vel, 3 * nb * sizeof(double), cudaMemcpyHostToDevice, s->st));
+        CK(cudaMemsetAsync(s->f, 0, (size_t)19 * s->Np * s->ssz, s->st));
+        for (int c = 0; c < 4; ++c) CK(cudaMemsetAsync(s->mom[c], 0, (size_t)s->Np * s->csz, s->st));
+        r = aux_init(s->prec, s->geom, dph, dden, dvel, s->we, s->f, s->mom[0], s->mom[1], s->mom[2], s->mom[3],
+                     s->st);
+        ++s->launches;
+        cudaError_t es = cudaStreamSynchronize(s->st);
+        cudaFree(dph); cudaFree(dden); cudaFree(dvel);
+        if (r) return fail(s, JLB_ERR_CUDA, std::string("init kernel: ") + cudaGetErrorString((cudaError_t)r));
+        CK(es);
+    } else {
+        s->nfluid = 0;
+    }
+    s->parity = 0;
+    s->init_done = true;
+    if (nfluid) *nfluid = cnt;
+    return JLB_OK;
+}
+
+int jlb_evolve(jlb_solver *s, uint32_t tsteps, const double g[3], double *den, double *vel, const double *acc,
+               uint32_t *tot) {
+    if (!s) return fail(s, JLB_ERR_INVALID_ARG, "NULL solver");
+    if (!s->init_done)
+        return fail(s, JLB_ERR_STATE, "Finalize solver initialization before calling evolve\n"
+                                      "(i.e. call first the method finalize_init)!");
+    if (!den || !vel) return fail(s, JLB_ERR_INVALID_ARG, "NULL den/vel");
+    if (g) {
+        for (int d = 0; d < 3; ++d) {
+            if (!std::isfinite(g[d])) return fail(s, JLB_ERR_INVALID_ARG, "Invalid gravity input.");
+            if (g[d] != s->g[d]) { s->g[d] = g[d]; ++s->args_version; }
+        }
+    }
+    if (s->nfluid < 1 || tsteps == 0) {
+        if (tot) *tot = s->tot;
+        return JLB_OK;
+    }
+    enforce_den_vel(s, den, vel);
+    // solid velocities: reclassify when any of them changed since the last call
+    bool changed = false;
+    for (size_t w = 0; w < s->wall_pos.size() && !changed; ++w) {
+        const double *u = vel + 3 * s->wall_pos[w];
+        changed = u[0] != s->wall_vel[3 * w] || u[1] != s->wall_vel[3 * w + 1] || u[2] != s->wall_vel[3 * w + 2];
+    }
+    if (changed) {
+        build_special(s, vel);
+        int r = upload_tables(s);
+        if (r) return r;
+    }
+    fill_dynamic(s, den, vel);
+    int r = upload_dynamic(s);
+    if (r) return r;
+    // acceleration field (read every step by the reference, jyulb/isothermal.pyx:1293-1295)
+    bool accf = false;
+    if (acc) {
+        for (int I = 1; I < s->NI - 1 && !accf; ++I)
+            for (int J = 1; J < s->NJ - 1 && !accf; ++J)
+                for (int K = 1; K < s->NK - 1; ++K) {
+                    const double *a = acc + 3 * fidx(s, I, J, K);
+                    if (a[0] != 0.0 || a[1] != 0.0 || a[2] != 0.0) { accf = true; break; }
+                }
+    }
+    if (accf) {
+        if (!s->acc) CK(cudaMalloc(&s->acc, (size_t)3 * s->Np * s->csz));
+        const double *da = (const double *)dev_view(acc);
+        if (da) {
+            CKR(aux_acc_upload(s->prec, s->geom, da, s->acc, s->st));
+            s->h2d_bytes += (uint64_t)s->N * 3 * sizeof(double);
+        } else {
+            double *tmp = nullptr;
+            CK(cudaMalloc(&tmp, (size_t)3 * s->NCNT * sizeof(double)));
+            cudaMemcpyAsync(tmp, acc, (size_t)3 * s->NCNT * sizeof(double), cudaMemcpyHostToDevice, s->st);
+            int rr = aux_acc_upload(s->prec, s->geom, tmp, s->acc, s->st);
+            cudaStreamSynchronize(s->st);
+            cudaFree(tmp);
+            CKR(rr);
+        }
+        ++s->launches;
+    }
+    if (accf != s->accf) { s->accf = accf; ++s->args_version; }
+    r = run_steps(s, tsteps, true);
+    if (r) return r;
+    r = download(s, den, vel);
+    if (r) return r;
+    s->tot += tsteps;
+    if (tot) *tot = s->tot;
+    return JLB_OK;
+}
+
+int jlb_step(jlb_solver *s, uint32_t tsteps, int write_moments) {
+    if (!s) return fail(s, JLB_ERR_INVALID_ARG, "NULL solver");
+    if (!s->init_done) return fail(s, JLB_ERR_STATE, "finalize_init has not been called");
+    if (s->nfluid < 1) return JLB_OK;
+    int r = run_steps(s, tsteps, write_moments != 0);
+    if (r) return r;
+    s->tot += tsteps;
+    return JLB_OK;
+}
+
+int jlb_download_moments(jlb_solver *s, double *den, double *vel) {
+    if (!s || !den || !vel) return fail(s, JLB_ERR_INVALID_ARG, "NULL argument");
+    if (!s->init_done) return fail(s, JLB_ERR_STATE, "finalize_init has not been called");
+    return download(s, den, vel);
+}
+
+int jlb_get_populations(jlb_solver *s, double *f) {
+    if (!s || !f) return fail(s, JLB_ERR_INVALID_ARG, "NULL argument");
+    if (!s->init_done) return fail(s, JLB_ERR_STATE, "finalize_init has not been called");
+    const size_t nb = (size_t)19 * s->N * sizeof(double);
+    double *tmp = nullptr;
+    CK(cudaMalloc(&tmp, nb));
+    int r = aux_readout(s->prec, s->geom, s->f, s->nmask, s->parity, s->M, s->d_sp_node, s->d_sp_wr, tmp, s->st);
+    s->launches += 1 + (s->M > 0);
+    cudaError_t e = r ? (cudaError_t)r : cudaMemcpyAsync(f, tmp, nb, cudaMemcpyDeviceToHost, s->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
+    cudaFree(tmp);
+    CK(e);
+    return JLB_OK;
+}
+
+int jlb_set_populations(jlb_solver *s, const double *f) {
+    if (!s || !f) return fail(s, JLB_ERR_INVALID_ARG, "NULL argument");
+    if (!s->init_done) return fail(s, JLB_ERR_STATE, "finalize_init has not been called");
+    const size_t nb = (size_t)19 * s->N * sizeof(double);
+    double *tmp = nullptr;
+    CK(cudaMalloc(&tmp, nb));
+    cudaError_t e = cudaMemcpyAsync(tmp, f, nb, cudaMemcpyHostToDevice, s->st);
+    if (e == cudaSuccess) e = (cudaError_t)aux_restore(s->prec, s->geom, s->f, s->nmask, tmp, s->st);
+    ++s->launches;
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
+    cudaFree(tmp);
+    CK(e);
+    s->parity = 0;
+    return JLB_OK;
+}
+
+int jlb_reduce(jlb_solver *s, double out[8]) {
+    if (!s || !out) return fail(s, JLB_ERR_INVALID_ARG, "NULL argument");
+    if (!s->init_done) return fail(s, JLB_ERR_STATE, "finalize_init has not been called");
+    CKR(aux_reduce(s->prec, s->geom, s->nmask, s->mom[0], s->mom[1], s->mom[2], s->mom[3], s->red_partial,
+                   s->red_blocks, s->red_out, s->st));
+    s->launches += 2;
+    CK(cudaMemcpyAsync(out, s->red_out, 8 * sizeof(double), cudaMemcpyDeviceToHost, s->st));
+    CK(cudaStreamSynchronize(s->st));
+    if (out[7] != 0.0) return fail(s, JLB_ERR_NUMERIC, "non-finite density or velocity found");
+    return JLB_OK;
+}
+
+uint32_t jlb_tot_tsteps(const jlb_solver *s) { return s ? s->tot : 0; }
+
+void jlb_rlx_prm(const jlb_solver *s, double out[2]) {
+    if (!s || !out) return;
+    out[0] = s->we;
+    out[1] = s->wo;
+}
+
+uint64_t jlb_kernel_launches(const jlb_solver *s) { return s ? s->launches : 0; }
+
+void jlb_transfer_bytes(const jlb_solver *s, uint64_t out[2]) {
+    if (!out) return;
+    out[0] = s ? s->h2d_bytes : 0;
+    out[1] = s ? s->d2h_bytes : 0;
+}
+
+const char *jlb_last_error(const jlb_solver *s) {
+    if (!s) return g_create_error.c_str();
+    return s->err.c_str();
+}
+
+const char *jlb_build_info(void) {
+    return "libjyulb_gb300: D3Q19 AA-pattern fused step for sm_103a; FP64 (reference arithmetic, no FMA), "
+           "FP32 shifted, FP16 storage; BGK/TRT/regularized; bounce-back, Ladd moving walls, Zou-He, "
+           "periodic, symmetric";
+}
+
+} // extern "C"

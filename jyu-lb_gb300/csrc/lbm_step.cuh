@@ -1,0 +1,265 @@
+// lbm_step.cuh -- the fused D3Q19 time step (stream + bounce-back + Zou-He +
+// collide + moments) for one AA half-pair, generic over the storage policy
+// and the collision physics.
+//
+// One launch per time step.  Blocks [0, nb_dense) sweep the lattice in
+// (k-fastest) rows: every fluid node that is not a boundary node streams with
+// plain neighbour arithmetic (periodic wrap for free) and halfway bounce-back
+// from its 19-bit link mask.  Blocks [nb_dense, grid) handle the boundary
+// nodes from a precomputed list: Zou-He faces, links that cross a symmetric
+// face, and links to moving solids (Ladd's term), each with explicit per-link
+// read/write element indices.  The two sets are disjoint and the AA pattern
+// makes every slot written by exactly the node that reads it, so both halves
+// run in one launch without synchronisation.
+#pragma once
+#include <cuda_runtime.h>
+#include <cuda_fp16.h>
+#include "lbm_common.h"
+
+namespace jlb {
+
+// lattice tables as constexpr functions of q (resolved at compile time in the
+// unrolled loops)
+__host__ __device__ constexpr int CX(int q) { return q < 5 ? -1 : (q >= 14 ? 1 : 0); }
+__host__ __device__ constexpr int CY(int q) {
+    return (q == 0 || q == 5 || q == 6 || q == 7 || q == 14) ? -1
+         : (q == 4 || q == 11 || q == 12 || q == 13 || q == 18) ? 1 : 0;
+}
+__host__ __device__ constexpr int CZ(int q) {
+    return (q == 1 || q == 5 || q == 8 || q == 11 || q == 15) ? -1
+         : (q == 3 || q == 7 || q == 10 || q == 13 || q == 17) ? 1 : 0;
+}
+__host__ __device__ constexpr int OPP(int q) { return 18 - q; }
+__host__ __device__ constexpr int NNZ(int q) {
+    return (CX(q) != 0) + (CY(q) != 0) + (CZ(q) != 0);
+}
+// weight class of q: 0 rest, 1 axis, 2 diagonal
+__host__ __device__ constexpr int WCLASS(int q) { return NNZ(q); }
+
+// ---------------------------------------------------------------------------
+// storage policies
+// ---------------------------------------------------------------------------
+struct StoreF64 {
+    using S = double;
+    using C = double;
+    static constexpr bool shifted = false;
+    template <int q> __device__ static C ld(const S *p) { return __ldg(p); }
+    template <int q> __device__ static C ldv(S v) { return v; }
+    template <int q> __device__ static void st(S *p, C v) { *p = v; }
+};
+
+struct StoreF32 {
+    using S = float;
+    using C = float;
+    static constexpr bool shifted = true; // holds f_q - w_q
+    template <int q> __device__ static C ld(const S *p) { return __ldg(p); }
+    template <int q> __device__ static C ldv(S v) { return v; }
+    template <int q> __device__ static void st(S *p, C v) { *p = v; }
+};
+
+// FP16 holds 2^12 * (f_q - w_q) / w_q
+struct StoreF16 {
+    using S = __half;
+    using C = float;
+    static constexpr bool shifted = true;
+    template <int q> __device__ static constexpr float dec() {
+        return WCLASS(q) == 0 ? (1.0f / 12288.0f) : WCLASS(q) == 1 ? (1.0f / 73728.0f) : (1.0f / 147456.0f);
+    }
+    template <int q> __device__ static constexpr float enc() {
+        return WCLASS(q) == 0 ? 12288.0f : WCLASS(q) == 1 ? 73728.0f : 147456.0f;
+    }
+    template <int q> __device__ static C ld(const S *p) {
+        return __half2float(*p) * dec<q>();
+    }
+    template <int q> __device__ static C ldv(S v) { return __half2float(v) * dec<q>(); }
+    template <int q> __device__ static void st(S *p, C v) { *p = __float2half_rn(v * enc<q>()); }
+};
+
+// compile-time loop
+template <int I, int N> struct Unroll {
+    template <class F> __device__ __forceinline__ static void run(F &&f) {
+        f.template operator()<I>();
+        Unroll<I + 1, N>::run(f);
+    }
+};
+template <int N> struct Unroll<N, N> {
+    template <class F> __device__ __forceinline__ static void run(F &&) {}
+};
+
+// ---------------------------------------------------------------------------
+// dense (interior / plain bounce-back / periodic) nodes
+// ---------------------------------------------------------------------------
+template <class ST, class PH, bool PSTEP, bool ACCF>
+__device__ __forceinline__ void dense_node(const StepArgs &a, int b) {
+    using S = typename ST::S;
+    using C = typename ST::C;
+    const int kb = b % a.kblocks;
+    const int rb = b / a.kblocks;
+    const int row = rb * a.by + (int)threadIdx.y;
+    const int k = kb * a.bx + (int)threadIdx.x;
+    if (row >= a.nx * a.ny || k >= a.nz) return;
+    const int i = row / a.ny;
+    const int j = row - i * a.ny;
+    const int64_t n = (int64_t)row * a.nz + k;
+    const uint32_t m = __ldg(a.nmask + n);
+    if (m & MASK_SKIP) return;
+
+    S *__restrict__ f = (S *)a.f;
+    const int64_t Np = a.Np;
+    C fv[Q];
+
+    // neighbour node offsets along each axis: index 0 -> -1, 1 -> 0, 2 -> +1
+    int64_t oi[3], oj[3], ok[3];
+    if (PSTEP) {
+        const int64_t sI = (int64_t)a.ny * a.nz, sJ = a.nz;
+        const int im = (i == 0) ? a.nx - 1 : i - 1, ip = (i + 1 == a.nx) ? 0 : i + 1;
+        const int jm = (j == 0) ? a.ny - 1 : j - 1, jp = (j + 1 == a.ny) ? 0 : j + 1;
+        const int km = (k == 0) ? a.nz - 1 : k - 1, kp = (k + 1 == a.nz) ? 0 : k + 1;
+        oi[0] = im * sI; oi[1] = i * sI; oi[2] = ip * sI;
+        oj[0] = jm * sJ; oj[1] = j * sJ; oj[2] = jp * sJ;
+        ok[0] = km;      ok[1] = k;      ok[2] = kp;
+    }
+
+    Unroll<0, Q>::run([&]<int q>() {
+        if (PSTEP) {
+            if (q == 9) {
+                fv[q] = ST::template ld<q>(f + 9 * Np + n);
+            } else if (m & (1u << q)) {
+                fv[q] = ST::template ld<q>(f + q * Np + n);
+            } else {
+                const int64_t src = oi[1 - CX(q)] + oj[1 - CY(q)] + ok[1 - CZ(q)];
+                fv[q] = ST::template ld<q>(f + OPP(q) * Np + src);
+            }
+        } else {
+            fv[q] = ST::template ld<q>(f + q * Np + n);
+        }
+    });
+
+    C ax, ay, az;
+    if (ACCF) {
+        const C *acc = (const C *)a.acc;
+        ax = (C)a.g[0] + __ldg(acc + n);
+        ay = (C)a.g[1] + __ldg(acc + Np + n);
+        az = (C)a.g[2] + __ldg(acc + 2 * Np + n);
+    } else {
+        ax = (C)a.g[0]; ay = (C)a.g[1]; az = (C)a.g[2];
+    }
+    C ux, uy, uz;
+    const C rho = PH::collide(fv, ax, ay, az, (C)a.w_e, (C)a.w_o, ux, uy, uz);
+
+    Unroll<0, Q>::run([&]<int q>() {
+        if (PSTEP) {
+            if (q == 9) {
+                ST::template st<q>(f + 9 * Np + n, fv[q]);
+            } else if (m & (1u << OPP(q))) {
+                ST::template st<q>(f + OPP(q) * Np + n, fv[q]);
+            } else {
+                const int64_t dst = oi[1 + CX(q)] + oj[1 + CY(q)] + ok[1 + CZ(q)];
+                ST::template st<q>(f + q * Np + dst, fv[q]);
+            }
+        } else {
+            ST::template st<OPP(q)>(f + OPP(q) * Np + n, fv[q]);
+        }
+    });
+
+    if (a.write_moments) {
+        ((C *)a.den)[n] = rho;
+        ((C *)a.ux)[n] = ux;
+        ((C *)a.uy)[n] = uy;
+        ((C *)a.uz)[n] = uz;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// boundary nodes (Zou-He, symmetric faces, moving solids)
+// ---------------------------------------------------------------------------
+template <class ST, class PH, bool PSTEP, bool ACCF>
+__device__ __forceinline__ void special_node(const StepArgs &a, int b) {
+    using S = typename ST::S;
+    using C = typename ST::C;
+    const int t = b * (int)(blockDim.x * blockDim.y) + (int)(threadIdx.y * blockDim.x + threadIdx.x);
+    const int M = a.M;
+    if (t >= M) return;
+    const int64_t n = __ldg(a.sp_node + t);
+    const uint32_t info = __ldg(a.sp_info + t);
+    S *__restrict__ f = (S *)a.f;
+    const int64_t Np = a.Np;
+    C *spden = (C *)a.sp_den;
+    const C dprev = spden[t];
+    C fv[Q];
+
+    Unroll<0, Q>::run([&]<int q>() {
+        const int64_t addr = PSTEP ? __ldg(a.sp_rd + (int64_t)q * M + t) : (int64_t)q * Np + n;
+        // the value read may belong to any slot; decode with the slot of q's
+        // source population (same weight class: mirrors and opposites keep it)
+        C v = ST::template ld<q>(f + addr);
+        if (q != 9 && (info & (1u << q)))
+            v = PH::template ladd<q>(v, dprev, (C)__ldg(a.sp_lw + (int64_t)q * M + t));
+        fv[q] = v;
+    });
+
+    const uint32_t faces = (info >> SP_FACE_SHIFT) & 0x3Fu;
+    if (faces) {
+        int slot = 0;
+#pragma unroll
+        for (int fc = 0; fc < 6; ++fc) {
+            if (faces & (1u << fc)) {
+                const double *bcd = a.sp_bc + (int64_t)(4 * slot) * M + t;
+                PH::zou_he(fc, a.bc[fc], bcd[0], bcd[M], bcd[2 * (int64_t)M], bcd[3 * (int64_t)M], fv);
+                slot = 1;
+            }
+        }
+    }
+
+    C ax, ay, az;
+    if (ACCF) {
+        const C *acc = (const C *)a.acc;
+        ax = (C)a.g[0] + __ldg(acc + n);
+        ay = (C)a.g[1] + __ldg(acc + Np + n);
+        az = (C)a.g[2] + __ldg(acc + 2 * Np + n);
+    } else {
+        ax = (C)a.g[0]; ay = (C)a.g[1]; az = (C)a.g[2];
+    }
+    C ux, uy, uz;
+    const C rho = PH::collide(fv, ax, ay, az, (C)a.w_e, (C)a.w_o, ux, uy, uz);
+
+    Unroll<0, Q>::run([&]<int q>() {
+        if (PSTEP) {
+            const int64_t addr = __ldg(a.sp_wr + (int64_t)q * M + t);
+            ST::template st<q>(f + addr, fv[q]);
+        } else {
+            ST::template st<OPP(q)>(f + OPP(q) * Np + n, fv[q]);
+        }
+    });
+    spden[t] = rho;
+    if (a.write_moments) {
+        ((C *)a.den)[n] = rho;
+        ((C *)a.ux)[n] = ux;
+        ((C *)a.uy)[n] = uy;
+        ((C *)a.uz)[n] = uz;
+    }
+}
+
+template <class ST, class PH, bool PSTEP, bool ACCF>
+__global__ void __launch_bounds__(128) lbm_step_kernel(const StepArgs a) {
+    const int b = (int)blockIdx.x;
+    if (b < a.nb_dense) dense_node<ST, PH, PSTEP, ACCF>(a, b);
+    else special_node<ST, PH, PSTEP, ACCF>(a, b - a.nb_dense);
+}
+
+template <class ST, template <int> class PH>
+int launch_step_impl(const StepArgs &a, int scheme, bool pstep, bool accf, int blocks, cudaStream_t st) {
+    dim3 blk(a.bx, a.by), grd(blocks);
+#define JLB_L(SCH, P, A) lbm_step_kernel<ST, PH<SCH>, P, A><<<grd, blk, 0, st>>>(a)
+#define JLB_S(SCH)                                   \
+    if (pstep) { if (accf) JLB_L(SCH, true, true); else JLB_L(SCH, true, false); } \
+    else { if (accf) JLB_L(SCH, false, true); else JLB_L(SCH, false, false); }
+    if (scheme == SCH_BGK) { JLB_S(SCH_BGK) }
+    else if (scheme == SCH_TRT) { JLB_S(SCH_TRT) }
+    else { JLB_S(SCH_REG) }
+#undef JLB_S
+#undef JLB_L
+    return (int)cudaGetLastError();
+}
+
+} // namespace jlb

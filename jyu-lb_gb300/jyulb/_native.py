@@ -1,0 +1,96 @@
+"""ctypes binding of libjyulb_gb300.so (C ABI declared in include/jyulb_gb300.h).
+
+The library is built in-tree by ``jyulb.build.build()`` (``__graft_entry__.build``)
+into this package directory.  Loading fails loudly: there is no CPU fallback
+for the time step.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libjyulb_gb300.so")
+
+JLB_OK = 0
+JLB_ERR_INVALID_ARG = -1
+JLB_ERR_STATE = -2
+JLB_ERR_CUDA = -3
+JLB_ERR_NOMEM = -4
+JLB_ERR_UNSUPPORTED = -5
+JLB_ERR_NUMERIC = -6
+
+# every symbol include/jyulb_gb300.h declares
+EXPORTED_SYMBOLS = (
+    "jlb_check_config", "jlb_create", "jlb_destroy", "jlb_finalize_init", "jlb_evolve",
+    "jlb_step", "jlb_download_moments", "jlb_get_populations", "jlb_set_populations",
+    "jlb_reduce", "jlb_tot_tsteps", "jlb_rlx_prm", "jlb_kernel_launches", "jlb_transfer_bytes",
+    "jlb_last_error",
+    "jlb_build_info",
+)
+
+
+class jlb_config(ctypes.Structure):
+    _fields_ = [
+        ("lat_size", ctypes.c_int32 * 3),
+        ("rlx_scheme", ctypes.c_int32),
+        ("kvisc", ctypes.c_double),
+        ("g", ctypes.c_double * 3),
+        ("bc", ctypes.c_int32 * 6),
+        ("precision", ctypes.c_int32),
+        ("trt_magic", ctypes.c_double),
+        ("stream", ctypes.c_void_p),
+    ]
+
+
+class EngineUnavailable(RuntimeError):
+    """The CUDA engine library is missing or cannot run here."""
+
+
+_lib = None
+
+
+def load() -> ctypes.CDLL:
+    """Load the engine library (raises EngineUnavailable if it is not built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise EngineUnavailable(
+            f"{LIB_PATH} is not built; run __graft_entry__.build() (nvcc, sm_103a)")
+    lib = ctypes.CDLL(LIB_PATH)
+    vp, dp = ctypes.c_void_p, ctypes.POINTER(ctypes.c_double)
+    u8p = ctypes.POINTER(ctypes.c_uint8)
+    cfgp = ctypes.POINTER(jlb_config)
+    sig = {
+        "jlb_check_config": (ctypes.c_int, [cfgp, ctypes.c_char_p, ctypes.c_size_t]),
+        "jlb_create": (ctypes.c_int, [cfgp, ctypes.POINTER(vp)]),
+        "jlb_destroy": (None, [vp]),
+        "jlb_finalize_init": (ctypes.c_int, [vp, u8p, dp, dp, ctypes.POINTER(ctypes.c_uint64)]),
+        "jlb_evolve": (ctypes.c_int, [vp, ctypes.c_uint32, dp, dp, dp, dp, ctypes.POINTER(ctypes.c_uint32)]),
+        "jlb_step": (ctypes.c_int, [vp, ctypes.c_uint32, ctypes.c_int]),
+        "jlb_download_moments": (ctypes.c_int, [vp, dp, dp]),
+        "jlb_get_populations": (ctypes.c_int, [vp, dp]),
+        "jlb_set_populations": (ctypes.c_int, [vp, dp]),
+        "jlb_reduce": (ctypes.c_int, [vp, dp]),
+        "jlb_tot_tsteps": (ctypes.c_uint32, [vp]),
+        "jlb_rlx_prm": (None, [vp, dp]),
+        "jlb_kernel_launches": (ctypes.c_uint64, [vp]),
+        "jlb_transfer_bytes": (None, [vp, ctypes.POINTER(ctypes.c_uint64)]),
+        "jlb_last_error": (ctypes.c_char_p, [vp]),
+        "jlb_build_info": (ctypes.c_char_p, []),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def dptr(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def u8ptr(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8))

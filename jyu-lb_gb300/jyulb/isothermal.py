@@ -1,0 +1,354 @@
+"""Lattice-Boltzmann solver for isothermal single-phase flows, D3Q19, on one
+GB300 GPU.
+
+Drop-in for ``jyulb.isothermal.Solver`` (jyulb/isothermal.pyx,
+jyulb/isothermal.pxd:38-114): same constructors, properties, update methods,
+getters and error behaviour; the time-step loop runs as fused AA-pattern CUDA
+kernels (libjyulb_gb300.so) instead of the reference's OpenMP pull loop.
+
+The solver owns halo-padded host arrays with the reference's layout --
+``phase`` (NI,NJ,NK) uint8, ``den`` (NI,NJ,NK), ``vel``/``acc`` (NI,NJ,NK,3)
+float64, k fastest -- and the getters return writable views of their
+interior.  They are page-locked when CUDA is present, so the GPU reads and
+writes them in place.  As in the reference:
+
+* ``phase`` is read by ``finalize_init``;
+* ``den``/``vel`` are the initial field, and ``evolve`` overwrites them on
+  fluid sites with the pre-collision density and u = j/den + a/2;
+* ``vel`` of solid sites are wall velocities (Ladd's moving bounce-back) and
+  ``den``/``vel`` of the Zou-He face layers are the boundary data; both are
+  re-read at every ``evolve`` call;
+* ``acc`` is added to gravity at every step (read at every ``evolve`` call
+  once a view of it has been handed out).
+
+Additions of this engine (keyword-only): ``precision`` (defs.FP64 / FP32 /
+FP16), ``trt_magic`` (TRT magic parameter; None keeps the reference's 3/16) and
+``stream`` (a cudaStream_t handle as int to run on; default: the engine's own),
+plus ``populations``, ``set_populations``, ``reduce``, ``save_state`` and
+``load_state``.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _native
+from .D3Q19 import D3Q19_H10, LVECS
+from .defs import (BGK, FACE_1X, FACE_1Y, FACE_1Z, FACE_X1, FACE_Y1, FACE_Z1, FIXED_DEN,
+                   FIXED_VEL, FP16, FP32, FP64, PERIODIC, REGULARIZATION, SOLID, SYMMETRIC,
+                   TRT, WALL, X, Y, Z)
+
+_ERRS = {
+    _native.JLB_ERR_INVALID_ARG: ValueError,
+    _native.JLB_ERR_STATE: RuntimeError,
+    _native.JLB_ERR_NUMERIC: FloatingPointError,
+}
+
+
+def _host_array(shape, dtype, fill):
+    """Page-locked (GPU-addressable) array when CUDA is usable, else plain."""
+    try:
+        import torch
+        if torch.cuda.is_available():
+            t = torch.empty(int(np.prod(shape)), dtype={np.uint8: torch.uint8, np.float64: torch.float64}[dtype],
+                            pin_memory=True)
+            a = t.numpy().reshape(shape)
+            a[...] = fill
+            return a
+    except Exception:
+        pass
+    return np.full(shape, fill, dtype=dtype)
+
+
+def check_bc(bc):
+    """Boundary-condition validation of the reference (jyulb/isothermal.pyx:378-426);
+    raises ValueError with the reference's messages."""
+    valid = (WALL, PERIODIC, FIXED_DEN, FIXED_VEL, SYMMETRIC)
+    fixed = (FIXED_DEN, FIXED_VEL)
+    for s in range(6):
+        if bc[s] not in valid:
+            raise ValueError('Invalid boundary condition input.')
+    for ax, name in ((0, 'x'), (1, 'y'), (2, 'z')):
+        a, b = bc[2 * ax], bc[2 * ax + 1]
+        if (a == PERIODIC or b == PERIODIC) and a != b:
+            raise ValueError(f'Invalid periodic bc setup (in {name}-dir.).')
+    fx = [bc[2 * ax] in fixed or bc[2 * ax + 1] in fixed for ax in range(3)]
+    for ax in range(3):
+        if fx[ax] and any(fx[o] for o in range(3) if o != ax):
+            raise ValueError('Invalid fixed variable bc setup.')
+
+
+class Solver:
+    """D3Q19 isothermal lattice-Boltzmann solver (see the module docstring)."""
+
+    def __init__(self, lat_size, rlx_scheme=BGK, kvisc=1.0 / 6.0, g=None, bc=None, *,
+                 precision=FP64, trt_magic=None, stream=None):
+        self.error_msg = ''
+        lat = [int(v) for v in np.asarray(lat_size).reshape(-1)[:3]]
+        # argument checks of jyulb/isothermal.pyx:196-230
+        if len(lat) < 3 or lat[X] < 1 or lat[Y] < 1 or lat[Z] < 1:
+            self.error_msg = 'Invalid lattice size input.'
+            raise ValueError(self.error_msg)
+        if rlx_scheme not in (BGK, TRT, REGULARIZATION):
+            self.error_msg = 'Invalid relaxation scheme input.'
+            raise ValueError(self.error_msg)
+        if not kvisc > 0.0:
+            self.error_msg = 'Invalid kinematic viscosity input.'
+            raise ValueError(self.error_msg)
+        if precision not in (FP64, FP32, FP16):
+            raise ValueError('Invalid precision input.')
+        self._g = np.zeros(3) if g is None else np.array([g[X], g[Y], g[Z]], dtype=np.float64)
+        if bc is None:
+            self._bc = [PERIODIC] * 6
+        else:
+            bcl = [int(b) for b in bc[:6]]
+            try:
+                check_bc(bcl)
+            except ValueError as e:
+                self.error_msg = str(e)
+                raise
+            self._bc = bcl
+        self.NI, self.NJ, self.NK = lat[X] + 2, lat[Y] + 2, lat[Z] + 2
+        self.NCNT = self.NI * self.NJ * self.NK
+        self.kvisc = float(kvisc)
+        self.rlx_scheme = int(rlx_scheme)
+        self.precision = int(precision)
+        self.trt_magic = None if trt_magic is None else float(trt_magic)
+        self._stream = stream
+        self.tot_tsteps = 0
+        self.init_done = 0
+        self.dvs = D3Q19_H10()
+        sh = (self.NI, self.NJ, self.NK)
+        self.phase = _host_array(sh, np.uint8, SOLID)
+        self.den = _host_array(sh, np.float64, 1.0)
+        self.vel = _host_array(sh + (3,), np.float64, 0.0)
+        self._acc = _host_array(sh + (3,), np.float64, 0.0)
+        self._acc_exposed = False
+        self.fluid_lsite_domain = None
+        # relaxation parameters (jyulb/isothermal.pyx:274-287)
+        tau_e = 0.5 + self.dvs.AS2 * self.kvisc
+        self.rlx_prm = np.zeros(LVECS)
+        self.rlx_prm[0] = 1.0 / tau_e
+        if rlx_scheme == TRT:
+            w = self.rlx_prm[0]
+            if self.trt_magic is None:
+                self.rlx_prm[1] = 8.0 * (2.0 - w) / (8.0 - w)
+            else:
+                self.rlx_prm[1] = 1.0 / (self.trt_magic / (tau_e - 0.5) + 0.5)
+        self.njump = np.array([(li * self.NJ + lj) * self.NK + lk for li, lj, lk in
+                               zip(self.dvs.LI, self.dvs.LJ, self.dvs.LK)], dtype=np.int32)
+        self._h = None
+        self._lib = None
+        self._create_engine()
+
+    # -- construction --------------------------------------------------------
+    def _create_engine(self):
+        try:
+            lib = _native.load()
+        except OSError as e:
+            raise _native.EngineUnavailable(f'cannot load the CUDA engine: {e}') from e
+        cfg = _native.jlb_config()
+        cfg.lat_size[:] = [self.NI - 2, self.NJ - 2, self.NK - 2]
+        cfg.rlx_scheme = self.rlx_scheme
+        cfg.kvisc = self.kvisc
+        cfg.g[:] = list(self._g)
+        cfg.bc[:] = self._bc
+        cfg.precision = self.precision
+        cfg.trt_magic = 0.0 if self.trt_magic is None else self.trt_magic
+        cfg.stream = None if self._stream is None else int(self._stream)
+        h = ctypes.c_void_p()
+        rc = lib.jlb_create(ctypes.byref(cfg), ctypes.byref(h))
+        if rc != _native.JLB_OK:
+            msg = lib.jlb_last_error(None).decode()
+            if rc == _native.JLB_ERR_INVALID_ARG:
+                raise ValueError(msg)
+            raise _native.EngineUnavailable(f'CUDA engine unavailable: {msg}')
+        self._lib = lib
+        self._h = h
+
+    def __del__(self):
+        h = getattr(self, '_h', None)
+        if h is not None and self._lib is not None:
+            self._lib.jlb_destroy(h)
+            self._h = None
+
+    @classmethod
+    def with_iflow(cls, phase, iden, ivel, rlx_scheme=BGK, kvisc=1.0 / 6.0, g=None, bc=None, **kw):
+        """Solver with the initial flow field prescribed (jyulb/isothermal.pyx:301-360)."""
+        phase = np.asarray(phase)
+        iden = np.asarray(iden)
+        ivel = np.asarray(ivel)
+        for ax, name in ((X, 'x'), (Y, 'y'), (Z, 'z')):
+            if iden.shape[ax] != phase.shape[ax] or ivel.shape[ax] != phase.shape[ax]:
+                raise ValueError('Invalid input for the initial flow field: '
+                                 f'array sizes do not match ({name}-dimension)!')
+        s = cls(np.array(phase.shape, dtype=np.int32), rlx_scheme, kvisc, g, bc, **kw)
+        s.phase[1:-1, 1:-1, 1:-1] = phase
+        s.den[1:-1, 1:-1, 1:-1] = iden
+        s.vel[1:-1, 1:-1, 1:-1, :] = ivel
+        return s
+
+    def _raise(self, rc):
+        msg = self._lib.jlb_last_error(self._h).decode()
+        raise _ERRS.get(rc, RuntimeError)(msg)
+
+    # -- properties ------------------------------------------------------------
+    @property
+    def gravity(self):
+        return self._g.copy()
+
+    @gravity.setter
+    def gravity(self, g):
+        self._g[:] = [g[X], g[Y], g[Z]]
+
+    @property
+    def g(self):
+        return self._g.copy()
+
+    @property
+    def bc(self):
+        return list(self._bc)
+
+    @property
+    def f1(self):
+        """Post-collision populations in the reference's Bundle-C layout
+        (NCNT*19 values, jyulb/isothermal.pyx:1532-1704); halo entries are 0."""
+        f = self.populations()
+        NI, NJ, NK, N = self.NI, self.NJ, self.NK, self.NCNT
+        full = np.zeros((LVECS, NI, NJ, NK))
+        full[:, 1:-1, 1:-1, 1:-1] = f
+        full = full.reshape(LVECS, N)
+        out = np.empty(LVECS * N)
+        out[:5 * N].reshape(N, 5)[:] = full[0:5].T
+        out[5 * N:14 * N].reshape(N, 9)[:] = full[5:14].T
+        out[14 * N:].reshape(N, 5)[:] = full[14:19].T
+        return out
+
+    # -- update methods --------------------------------------------------------
+    def finalize_init(self):
+        """Finish the set-up; returns the number of fluid sites
+        (jyulb/isothermal.pyx:1333-1365)."""
+        if self.error_occured():
+            raise RuntimeError('Invalid solver setup: finalization aborted!')
+        n = ctypes.c_uint64()
+        rc = self._lib.jlb_finalize_init(self._h, _native.u8ptr(self.phase), _native.dptr(self.den),
+                                         _native.dptr(self.vel), ctypes.byref(n))
+        if rc != _native.JLB_OK:
+            self._raise(rc)
+        interior = self.phase[1:-1, 1:-1, 1:-1]
+        if n.value >= 1:
+            self.fluid_lsite_domain = np.array(np.nonzero(interior), dtype=np.uint32)
+        self.init_done = 1
+        return int(n.value)
+
+    def evolve(self, tsteps):
+        """Advance ``tsteps`` time steps; returns the total step count
+        (jyulb/isothermal.pyx:1370-1418)."""
+        if self.error_occured():
+            raise RuntimeError('Invalid solver setup: evolve aborted!')
+        if self.init_done == 0:
+            raise RuntimeError('Finalize solver initialization before calling evolve\n'
+                               '(i.e. call first the method finalize_init)!')
+        if self.fluid_lsite_domain is None:
+            return self.tot_tsteps
+        tot = ctypes.c_uint32()
+        acc = _native.dptr(self._acc) if self._acc_exposed else None
+        rc = self._lib.jlb_evolve(self._h, int(tsteps), _native.dptr(self._g), _native.dptr(self.den),
+                                  _native.dptr(self.vel), acc, ctypes.byref(tot))
+        if rc != _native.JLB_OK:
+            self._raise(rc)
+        self.tot_tsteps = int(tot.value)
+        return self.tot_tsteps
+
+    # -- status ------------------------------------------------------------------
+    def error_occured(self):
+        return len(self.error_msg)
+
+    # -- equation of state (jyulb/isothermal.pyx:1431-1458) --------------------
+    def eos_den2p(self, den):
+        return self.dvs.INV_AS2 * den
+
+    def eos_p2den(self, p):
+        return self.dvs.AS2 * p
+
+    # -- getters (jyulb/isothermal.pyx:1465-1527) ------------------------------
+    def get_phase(self):
+        return self.phase[1:-1, 1:-1, 1:-1]
+
+    @property
+    def acc(self):
+        """Halo-padded acceleration field; once handed out it is re-read at
+        every evolve call."""
+        self._acc_exposed = True
+        return self._acc
+
+    def get_acc(self):
+        self._acc_exposed = True
+        return self._acc[1:-1, 1:-1, 1:-1, :]
+
+    def get_vel(self):
+        return self.vel[1:-1, 1:-1, 1:-1, :]
+
+    def get_den(self):
+        return self.den[1:-1, 1:-1, 1:-1]
+
+    def get_fluid_lat_sites(self):
+        return self.fluid_lsite_domain
+
+    # -- engine additions --------------------------------------------------------
+    def populations(self):
+        """Post-collision populations of the latest step, (19, nx, ny, nz) FP64,
+        lattice vectors in the reference's order."""
+        self._need_init()
+        f = np.empty((LVECS, self.NI - 2, self.NJ - 2, self.NK - 2))
+        rc = self._lib.jlb_get_populations(self._h, _native.dptr(f))
+        if rc != _native.JLB_OK:
+            self._raise(rc)
+        return f
+
+    def set_populations(self, f):
+        """Overwrite the populations with post-collision values (same layout)."""
+        self._need_init()
+        f = np.ascontiguousarray(f, dtype=np.float64)
+        if f.shape != (LVECS, self.NI - 2, self.NJ - 2, self.NK - 2):
+            raise ValueError('populations must have shape (19, nx, ny, nz)')
+        rc = self._lib.jlb_set_populations(self._h, _native.dptr(f))
+        if rc != _native.JLB_OK:
+            self._raise(rc)
+
+    def save_state(self):
+        """Snapshot for restart: populations, den/vel and the step count."""
+        return {'f': self.populations(), 'den': self.den.copy(), 'vel': self.vel.copy(),
+                'tot_tsteps': self.tot_tsteps}
+
+    def load_state(self, state):
+        self.set_populations(state['f'])
+        self.den[...] = state['den']
+        self.vel[...] = state['vel']
+        self.tot_tsteps = int(state['tot_tsteps'])
+
+    def reduce(self):
+        """FP64 sums over fluid sites of the last stored moments: mass,
+        momentum (den*u) and velocity."""
+        self._need_init()
+        out = np.zeros(8)
+        rc = self._lib.jlb_reduce(self._h, _native.dptr(out))
+        if rc != _native.JLB_OK:
+            self._raise(rc)
+        return {'mass': out[0], 'momentum': out[1:4].copy(), 'vel_sum': out[4:7].copy()}
+
+    @property
+    def kernel_launches(self):
+        return int(self._lib.jlb_kernel_launches(self._h))
+
+    @property
+    def transfer_bytes(self):
+        """(host-to-device, device-to-host) bytes moved by the engine so far."""
+        out = (ctypes.c_uint64 * 2)()
+        self._lib.jlb_transfer_bytes(self._h, out)
+        return int(out[0]), int(out[1])
+
+    def _need_init(self):
+        if not self.init_done:
+            raise RuntimeError('finalize_init has not been called')
