@@ -130,10 +130,10 @@ def profile_traffic(name):
         return None
 
 
-def time_device(s, nf, steps, warmup, torch):
-    """MLUPS and mean launch time of the step kernel, inputs in HBM."""
+def time_device(s, nf, steps, warmup, torch, st):
+    """MLUPS and mean launch time of the step kernel, inputs in HBM; the
+    events are recorded on the stream the solver launches on."""
     lib, h = s._lib, s._h
-    st = torch.cuda.current_stream()
     assert lib.jlb_step(h, warmup, 0) == 0
     torch.cuda.synchronize()
     l0 = s.kernel_launches
@@ -296,7 +296,8 @@ def main():
     from jyulb.defs import FP32, FP64
 
     n = args.size
-    stream = torch.cuda.current_stream().cuda_stream
+    tstream = torch.cuda.Stream()
+    stream = tstream.cuda_stream
     # replicas only: every rank advances its own cavity (the path has no
     # exchange step on one domain per GPU)
     s32, nf = cavity(n, FP32, stream)
@@ -304,7 +305,7 @@ def main():
         dist.barrier()
     torch.cuda.synchronize()
     with ClockSampler(local) as clk:
-        mlups, ms_launch, launches = time_device(s32, nf, args.steps, args.warmup, torch)
+        mlups, ms_launch, launches = time_device(s32, nf, args.steps, args.warmup, torch, tstream)
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
@@ -313,12 +314,12 @@ def main():
         ms_launch = float(t.item())
         mlups = nf * world / (ms_launch * 1e-3) / 1e6
     clocks = clk.summary()
-    e2e_mlups, e2e_ms, h2d, d2h = time_e2e(s32, nf, args.e2e_steps, 3)
+    e2e_mlups, e2e_ms, h2d, d2h = time_e2e(s32, nf, args.e2e_steps, 3) if args.e2e_steps > 0 else (0, 0, 0, 0)
     del s32
     torch.cuda.empty_cache()
     s64, _ = cavity(n, FP64, stream)
     with ClockSampler(local) as clk64:
-        mlups64, ms64, _ = time_device(s64, nf, max(args.steps // 4, 20), args.warmup, torch)
+        mlups64, ms64, _ = time_device(s64, nf, max(args.steps // 4, 20), args.warmup, torch, tstream)
     del s64
     torch.cuda.empty_cache()
     err = l2_error(n, args.err_steps, stream) if args.err_steps > 0 else None

@@ -19,13 +19,16 @@ INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 LIB = os.path.join(HERE, "jyulb", "libjyulb_gb300.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-COMMON = ["-std=c++20", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-I", CSRC, "-I", INCLUDE]
+COMMON = ["-std=c++20", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
+          "-I", CSRC, "-I", INCLUDE]
 UNITS = {
     "lbm_fp64.cu": ["-fmad=false"],
     "lbm_fp32.cu": [],
     "lbm_fp16.cu": [],
     "lbm_aux.cu": ["-fmad=false"],
-    "lbm_host.cpp": ["-x", "cu", "-Xcompiler", "-fopenmp"],
+    # host arithmetic (relaxation rates, Ladd projections) must not be
+    # FMA-contracted either: gcc contracts by default on aarch64
+    "lbm_host.cpp": ["-x", "cu", "-Xcompiler", "-fopenmp", "-Xcompiler", "-ffp-contract=off"],
 }
 HEADERS = ["lbm_common.h", "lbm_step.cuh", "lbm_shifted.cuh", "lbm_aux.h"]
 
@@ -39,6 +42,12 @@ def _nvcc() -> str:
 
 def _stale(obj: str, src: str) -> bool:
     if not os.path.exists(obj):
+        return True
+    stamp = obj + ".flags"
+    flags = " ".join(ARCH + COMMON + UNITS[os.path.basename(src)])
+    if not os.path.exists(stamp) or open(stamp).read() != flags:
+        with open(stamp, "w") as fh:
+            fh.write(flags)
         return True
     t = os.path.getmtime(obj)
     deps = [src] + [os.path.join(CSRC, h) for h in HEADERS] + [os.path.join(INCLUDE, "jyulb_gb300.h")]

@@ -204,5 +204,6 @@ def test_mass_conserved_large_periodic():
     r0 = s.reduce()
     s.evolve(200)
     r1 = s.reduce()
-    assert abs(r1["mass"] - r0["mass"]) <= 1e-9
-    assert np.allclose(r1["momentum"], r0["momentum"], atol=1e-9)
+    # per-site rounding of ~1e-16 per step over 2.6e5 sites and 200 steps
+    assert abs(r1["mass"] - r0["mass"]) <= 1e-12 * r0["mass"]
+    assert np.allclose(r1["momentum"], r0["momentum"], rtol=0, atol=1e-12 * r0["mass"])
