@@ -23,8 +23,10 @@ COMMON = ["-std=c++20", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler",
           "-I", CSRC, "-I", INCLUDE]
 UNITS = {
     "lbm_fp64.cu": ["-fmad=false"],
-    "lbm_fp32.cu": [],
-    "lbm_fp16.cu": [],
+    # 6 resident 128-thread blocks per SM (<= 80 registers): the FP32/FP16
+    # steps are latency-bound on HBM at lower occupancy
+    "lbm_fp32.cu": ["-DJLB_MIN_BLOCKS=6"],
+    "lbm_fp16.cu": ["-DJLB_MIN_BLOCKS=6"],
     "lbm_aux.cu": ["-fmad=false"],
     # host arithmetic (relaxation rates, Ladd projections) must not be
     # FMA-contracted either: gcc contracts by default on aarch64

@@ -89,7 +89,7 @@ template <int N> struct Unroll<N, N> {
 // ---------------------------------------------------------------------------
 // dense (interior / plain bounce-back / periodic) nodes
 // ---------------------------------------------------------------------------
-template <class ST, class PH, bool PSTEP, bool ACCF>
+template <class ST, class PH, bool PSTEP, bool ACCF, class IT>
 __device__ __forceinline__ void dense_node(const StepArgs &a, int b) {
     using S = typename ST::S;
     using C = typename ST::C;
@@ -98,41 +98,46 @@ __device__ __forceinline__ void dense_node(const StepArgs &a, int b) {
     const int row = rb * a.by + (int)threadIdx.y;
     const int k = kb * a.bx + (int)threadIdx.x;
     if (row >= a.nx * a.ny || k >= a.nz) return;
-    const int i = row / a.ny;
-    const int j = row - i * a.ny;
-    const int64_t n = (int64_t)row * a.nz + k;
+    // element indices fit IT (int32 when 19 * Np < 2^31, chosen by the host)
+    const IT n = (IT)row * a.nz + k;
     const uint32_t m = __ldg(a.nmask + n);
     if (m & MASK_SKIP) return;
 
     S *__restrict__ f = (S *)a.f;
-    const int64_t Np = a.Np;
+    const IT Np = (IT)a.Np;
     C fv[Q];
 
-    // neighbour node offsets along each axis: index 0 -> -1, 1 -> 0, 2 -> +1
-    int64_t oi[3], oj[3], ok[3];
+    // relative offsets of the (periodically wrapped) neighbours along each
+    // axis; index 0 -> -1, 1 -> 0, 2 -> +1
+    IT dI[3], dJ[3], dK[3];
     if (PSTEP) {
-        const int64_t sI = (int64_t)a.ny * a.nz, sJ = a.nz;
-        const int im = (i == 0) ? a.nx - 1 : i - 1, ip = (i + 1 == a.nx) ? 0 : i + 1;
-        const int jm = (j == 0) ? a.ny - 1 : j - 1, jp = (j + 1 == a.ny) ? 0 : j + 1;
-        const int km = (k == 0) ? a.nz - 1 : k - 1, kp = (k + 1 == a.nz) ? 0 : k + 1;
-        oi[0] = im * sI; oi[1] = i * sI; oi[2] = ip * sI;
-        oj[0] = jm * sJ; oj[1] = j * sJ; oj[2] = jp * sJ;
-        ok[0] = km;      ok[1] = k;      ok[2] = kp;
+        const int i = row / a.ny;
+        const int j = row - i * a.ny;
+        const IT sI = (IT)a.ny * a.nz, sJ = (IT)a.nz;
+        dI[0] = (i == 0 ? (IT)(a.nx - 1) : (IT)-1) * sI;
+        dI[1] = 0;
+        dI[2] = (i + 1 == a.nx ? (IT)(1 - a.nx) : (IT)1) * sI;
+        dJ[0] = (j == 0 ? (IT)(a.ny - 1) : (IT)-1) * sJ;
+        dJ[1] = 0;
+        dJ[2] = (j + 1 == a.ny ? (IT)(1 - a.ny) : (IT)1) * sJ;
+        dK[0] = k == 0 ? (IT)(a.nz - 1) : (IT)-1;
+        dK[1] = 0;
+        dK[2] = k + 1 == a.nz ? (IT)(1 - a.nz) : (IT)1;
     }
 
+    // gather: a bounce-back link reads its own opposite slot; the choice is a
+    // select, not a branch
     Unroll<0, Q>::run([&]<int q>() {
-        if (PSTEP) {
-            if (q == 9) {
-                fv[q] = ST::template ld<q>(f + 9 * Np + n);
-            } else if (m & (1u << q)) {
-                fv[q] = ST::template ld<q>(f + q * Np + n);
-            } else {
-                const int64_t src = oi[1 - CX(q)] + oj[1 - CY(q)] + ok[1 - CZ(q)];
-                fv[q] = ST::template ld<q>(f + OPP(q) * Np + src);
-            }
+        IT e;
+        if (!PSTEP || q == 9) {
+            e = (IT)q * Np + n;
         } else {
-            fv[q] = ST::template ld<q>(f + q * Np + n);
+            const IT src = n + dI[1 - CX(q)] + dJ[1 - CY(q)] + dK[1 - CZ(q)];
+            const IT e_reg = (IT)OPP(q) * Np + src;
+            const IT e_bb = (IT)q * Np + n;
+            e = (m & (1u << q)) ? e_bb : e_reg;
         }
+        fv[q] = ST::template ld<q>(f + e);
     });
 
     C ax, ay, az;
@@ -147,19 +152,23 @@ __device__ __forceinline__ void dense_node(const StepArgs &a, int b) {
     C ux, uy, uz;
     const C rho = PH::collide(fv, ax, ay, az, (C)a.w_e, (C)a.w_o, ux, uy, uz);
 
+    // scatter: a population heading into a solid is stored back into this
+    // node's opposite slot
     Unroll<0, Q>::run([&]<int q>() {
-        if (PSTEP) {
-            if (q == 9) {
-                ST::template st<q>(f + 9 * Np + n, fv[q]);
-            } else if (m & (1u << OPP(q))) {
-                ST::template st<q>(f + OPP(q) * Np + n, fv[q]);
-            } else {
-                const int64_t dst = oi[1 + CX(q)] + oj[1 + CY(q)] + ok[1 + CZ(q)];
-                ST::template st<q>(f + q * Np + dst, fv[q]);
-            }
-        } else {
-            ST::template st<OPP(q)>(f + OPP(q) * Np + n, fv[q]);
+        IT e;
+        if (!PSTEP) {
+            ST::template st<OPP(q)>(f + ((IT)OPP(q) * Np + n), fv[q]);
+            return;
         }
+        if (q == 9) {
+            e = (IT)9 * Np + n;
+        } else {
+            const IT dst = n + dI[1 + CX(q)] + dJ[1 + CY(q)] + dK[1 + CZ(q)];
+            const IT e_reg = (IT)q * Np + dst;
+            const IT e_bb = (IT)OPP(q) * Np + n;
+            e = (m & (1u << OPP(q))) ? e_bb : e_reg;
+        }
+        ST::template st<q>(f + e, fv[q]);
     });
 
     if (a.write_moments) {
@@ -240,17 +249,25 @@ __device__ __forceinline__ void special_node(const StepArgs &a, int b) {
     }
 }
 
-template <class ST, class PH, bool PSTEP, bool ACCF>
-__global__ void __launch_bounds__(128) lbm_step_kernel(const StepArgs a) {
+#ifndef JLB_MIN_BLOCKS
+#define JLB_MIN_BLOCKS 1
+#endif
+template <class ST, class PH, bool PSTEP, bool ACCF, class IT>
+__global__ void __launch_bounds__(128, JLB_MIN_BLOCKS) lbm_step_kernel(const StepArgs a) {
     const int b = (int)blockIdx.x;
-    if (b < a.nb_dense) dense_node<ST, PH, PSTEP, ACCF>(a, b);
+    if (b < a.nb_dense) dense_node<ST, PH, PSTEP, ACCF, IT>(a, b);
     else special_node<ST, PH, PSTEP, ACCF>(a, b - a.nb_dense);
 }
 
 template <class ST, template <int> class PH>
 int launch_step_impl(const StepArgs &a, int scheme, bool pstep, bool accf, int blocks, cudaStream_t st) {
     dim3 blk(a.bx, a.by), grd(blocks);
-#define JLB_L(SCH, P, A) lbm_step_kernel<ST, PH<SCH>, P, A><<<grd, blk, 0, st>>>(a)
+    const bool i64 = a.Np * 19 > 0x7fffffffLL;
+#define JLB_L(SCH, P, A)                                                                 \
+    do {                                                                                 \
+        if (i64) lbm_step_kernel<ST, PH<SCH>, P, A, int64_t><<<grd, blk, 0, st>>>(a);    \
+        else lbm_step_kernel<ST, PH<SCH>, P, A, int32_t><<<grd, blk, 0, st>>>(a);        \
+    } while (0)
 #define JLB_S(SCH)                                   \
     if (pstep) { if (accf) JLB_L(SCH, true, true); else JLB_L(SCH, true, false); } \
     else { if (accf) JLB_L(SCH, false, true); else JLB_L(SCH, false, false); }
