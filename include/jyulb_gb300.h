@@ -119,6 +119,27 @@ int jlb_set_populations(jlb_solver *s, const double *f);
  * out[7] = number of non-finite den/u values found. */
 int jlb_reduce(jlb_solver *s, double out[8]);
 
+/* Allocation-free variant of jlb_reduce, for callers that cannot call
+ * cudaMalloc (code inside another framework's memory pool, hosts that forbid
+ * allocation after start-up, drivers that budget device memory themselves).
+ * It has no counterpart in the reference.
+ *   nmask            n_sites node masks; sites with bit 31 set are skipped
+ *   den, ux, uy, uz  n_sites moments: double for JLB_FP64, float holding
+ *                    den - 1 (and u) for JLB_FP32 / JLB_FP16
+ *   out              8 doubles in device-writable memory, same meaning as
+ *                    jlb_reduce's out
+ *   stream           cudaStream_t (NULL: legacy default stream); the call
+ *                    only enqueues work, synchronise before reading out
+ * All pointers are device-accessible.  n_sites may be at most 2^28 (268435456)
+ * sites; larger or non-positive sizes return JLB_ERR_INVALID_ARG.  Scratch is
+ * a static device array of 256 KiB that every GPU loading the library keeps
+ * until the process exits; the first call on each device looks up its address
+ * and should therefore come before any stream capture.  All calls share that
+ * array (each call writes every partial it reads), so calls that overlap on
+ * the GPU race: serialise them, e.g. on one stream. */
+int jlb_reduce_moments_noalloc(const uint32_t *nmask, const void *den, const void *ux, const void *uy,
+                               const void *uz, int64_t n_sites, int32_t precision, double *out, void *stream);
+
 /* number of steps taken since finalize (Solver.tot_tsteps) */
 uint32_t jlb_tot_tsteps(const jlb_solver *s);
 

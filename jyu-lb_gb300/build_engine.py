@@ -28,6 +28,7 @@ UNITS = {
     "lbm_fp32.cu": ["-DJLB_MIN_BLOCKS=6"],
     "lbm_fp16.cu": ["-DJLB_MIN_BLOCKS=6"],
     "lbm_aux.cu": ["-fmad=false"],
+    "lbm_noalloc.cu": [],
     # host arithmetic (relaxation rates, Ladd projections) must not be
     # FMA-contracted either: gcc contracts by default on aarch64
     "lbm_host.cpp": ["-x", "cu", "-Xcompiler", "-fopenmp", "-Xcompiler", "-ffp-contract=off"],
