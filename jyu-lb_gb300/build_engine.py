@@ -33,7 +33,7 @@ UNITS = {
     # FMA-contracted either: gcc contracts by default on aarch64
     "lbm_host.cpp": ["-x", "cu", "-Xcompiler", "-fopenmp", "-Xcompiler", "-ffp-contract=off"],
 }
-HEADERS = ["lbm_common.h", "lbm_step.cuh", "lbm_shifted.cuh", "lbm_aux.h"]
+HEADERS = ["lbm_common.h", "lbm_step.cuh", "lbm_step_tma.cuh", "lbm_shifted.cuh", "lbm_aux.h"]
 
 
 def _nvcc() -> str:

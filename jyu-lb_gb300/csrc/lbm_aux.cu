@@ -197,20 +197,42 @@ __global__ void restore_kernel(AuxGeom g, typename ST::S *f, const uint32_t *nma
 // ---------------------------------------------------------------------------
 // moments -> host arrays (mapped memory), acceleration upload
 // ---------------------------------------------------------------------------
+// One block per chunk of DL_TILE sites of a k-row.  The (NI,NJ,NK,3) velocity
+// layout is assembled in shared memory first so that every warp store to the
+// host covers 256 contiguous bytes: NVLink-C2C writes run ~3.5x faster that
+// way than with one strided 8-byte store per component.  Solid sites keep
+// their host values (the caller's wall velocities).
+constexpr int DL_TILE = 256;
+
 template <class C, bool SHIFTED>
-__global__ void download_kernel(AuxGeom g, const uint32_t *nmask, const C *den, const C *ux, const C *uy,
-                                const C *uz, double *hden, double *hvel) {
-    const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (n >= g.N) return;
-    if (nmask[n] & MASK_SOLID) return;
-    const int i = (int)(n / ((int64_t)g.ny * g.nz));
-    const int rem = (int)(n - (int64_t)i * g.ny * g.nz);
-    const int j = rem / g.nz, k = rem - (rem / g.nz) * g.nz;
-    const int64_t fn = full_idx(g, i + 1, j + 1, k + 1);
-    hden[fn] = SHIFTED ? 1.0 + (double)den[n] : (double)den[n];
-    hvel[3 * fn] = (double)ux[n];
-    hvel[3 * fn + 1] = (double)uy[n];
-    hvel[3 * fn + 2] = (double)uz[n];
+__global__ void __launch_bounds__(DL_TILE) download_kernel(AuxGeom g, int kchunks, const uint32_t *nmask,
+                                                           const C *den, const C *ux, const C *uy, const C *uz,
+                                                           double *hden, double *hvel) {
+    __shared__ double sv[3 * DL_TILE];
+    __shared__ unsigned char sfl[DL_TILE];
+    const int64_t rowc = blockIdx.x;
+    const int64_t row = rowc / kchunks;
+    const int k0 = (int)(rowc - row * kchunks) * DL_TILE;
+    const int i = (int)(row / g.ny), j = (int)(row - (int64_t)i * g.ny);
+    const int cnt = min(DL_TILE, g.nz - k0);
+    const int t = threadIdx.x;
+    const int64_t n = row * g.nz + k0 + t;
+    const int64_t fn0 = full_idx(g, i + 1, j + 1, k0 + 1);
+    bool fl = false;
+    if (t < cnt) {
+        fl = !(nmask[n] & MASK_SOLID);
+        if (fl) {
+            hden[fn0 + t] = SHIFTED ? 1.0 + (double)den[n] : (double)den[n];
+            sv[3 * t] = (double)ux[n];
+            sv[3 * t + 1] = (double)uy[n];
+            sv[3 * t + 2] = (double)uz[n];
+        }
+        sfl[t] = fl;
+    }
+    __syncthreads();
+    double *hv = hvel + 3 * fn0;
+    for (int w = t; w < 3 * cnt; w += DL_TILE)
+        if (sfl[w / 3]) hv[w] = sv[w];
 }
 
 template <class C>
@@ -319,13 +341,16 @@ int aux_restore(int prec, const AuxGeom &g, void *f, const uint32_t *nmask, cons
 
 int aux_download(int prec, const AuxGeom &g, const uint32_t *nmask, const void *den, const void *ux,
                  const void *uy, const void *uz, double *hden, double *hvel, cudaStream_t st) {
-    const unsigned b = nblk(g.N, 256);
+    const int kchunks = (g.nz + DL_TILE - 1) / DL_TILE;
+    const unsigned b = (unsigned)((int64_t)g.nx * g.ny * kchunks);
     if (prec == PREC_FP64)
-        download_kernel<double, false><<<b, 256, 0, st>>>(g, nmask, (const double *)den, (const double *)ux,
-                                                          (const double *)uy, (const double *)uz, hden, hvel);
+        download_kernel<double, false><<<b, DL_TILE, 0, st>>>(g, kchunks, nmask, (const double *)den,
+                                                              (const double *)ux, (const double *)uy,
+                                                              (const double *)uz, hden, hvel);
     else
-        download_kernel<float, true><<<b, 256, 0, st>>>(g, nmask, (const float *)den, (const float *)ux,
-                                                        (const float *)uy, (const float *)uz, hden, hvel);
+        download_kernel<float, true><<<b, DL_TILE, 0, st>>>(g, kchunks, nmask, (const float *)den,
+                                                            (const float *)ux, (const float *)uy,
+                                                            (const float *)uz, hden, hvel);
     return (int)cudaGetLastError();
 }
 

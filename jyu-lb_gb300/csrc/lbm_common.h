@@ -30,6 +30,13 @@ constexpr uint32_t MASK_SPECIAL = 1u << 30;    // handled by the boundary-node p
 constexpr uint32_t MASK_SOLID = 1u << 31;      // not a fluid node
 constexpr uint32_t MASK_SKIP = MASK_SPECIAL | MASK_SOLID;
 
+// node classes (uint8 per node); the dense sweep reads the 32-bit mask only
+// for CLS_WALL nodes
+constexpr uint8_t CLS_PLAIN = 0;   // fluid, no bounce-back link
+constexpr uint8_t CLS_WALL = 1;    // fluid with bounce-back links
+constexpr uint8_t CLS_SPECIAL = 2; // boundary-node path
+constexpr uint8_t CLS_SOLID = 3;   // not a fluid node
+
 // boundary-node info bits
 constexpr uint32_t SP_LADD_SHIFT = 0;  // bits 0..18: link has a moving-wall term
 constexpr uint32_t SP_FACE_SHIFT = 20; // bits 20..25: node lies on fixed face f
@@ -43,6 +50,7 @@ struct StepArgs {
     int64_t Np;           // slot stride
     int nx, ny, nz;
     const uint32_t *nmask;
+    const uint8_t *ncls;  // per-node class: CLS_* below (1 byte read per node)
     void *den, *ux, *uy, *uz; // moments (compute type); den holds rho-1 for shifted storage
     const void *acc;      // optional acceleration field, 3 * Np (compute type), SoA
     double g[3];          // uniform gravity
@@ -68,5 +76,14 @@ struct StepArgs {
 int launch_step_fp64(const StepArgs &a, int scheme, bool pstep, bool accf, int blocks, cudaStream_t st);
 int launch_step_fp32(const StepArgs &a, int scheme, bool pstep, bool accf, int blocks, cudaStream_t st);
 int launch_step_fp16(const StepArgs &a, int scheme, bool pstep, bool accf, int blocks, cudaStream_t st);
+// bulk-copy staged variants (lbm_step_tma.cuh): persistent grid over
+// `ntiles` row tiles of 128 sites, then `nsb` boundary-node blocks; a
+// timed-out mbarrier wait sets *err
+int launch_step_tma_fp32(const StepArgs &a, int scheme, bool pstep, bool accf, int grid, int ntiles, int nsb,
+                         int *err, cudaStream_t st);
+int launch_step_tma_fp16(const StepArgs &a, int scheme, bool pstep, bool accf, int grid, int ntiles, int nsb,
+                         int *err, cudaStream_t st);
+int tma_blocks_per_sm_fp32(int scheme);
+int tma_blocks_per_sm_fp16(int scheme);
 
 } // namespace jlb

@@ -15,6 +15,7 @@
 #include <omp.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -64,6 +65,7 @@ struct jlb_solver {
     // device state
     void *f = nullptr;
     uint32_t *nmask = nullptr;
+    uint8_t *ncls = nullptr;
     void *mom[4] = {nullptr, nullptr, nullptr, nullptr};
     void *acc = nullptr;
     double *red_partial = nullptr, *red_out = nullptr;
@@ -78,6 +80,7 @@ struct jlb_solver {
     // host bookkeeping
     std::vector<uint8_t> phase;      // halo-padded snapshot after the halo rules
     std::vector<uint32_t> hmask;     // Np entries
+    std::vector<uint8_t> hcls;       // Np node classes derived from hmask
     std::vector<int64_t> wall_pos;   // solid positions next to fluid (halo-padded index)
     std::vector<double> wall_vel;    // their velocities at the last classification
     std::vector<int64_t> sp_node;
@@ -96,11 +99,16 @@ struct jlb_solver {
     double g[3] = {0, 0, 0};
     uint64_t launches = 0;
     uint64_t h2d_bytes = 0, d2h_bytes = 0; // host<->device traffic issued by the runtime
+    double host_t[6] = {0, 0, 0, 0, 0, 0};  // cumulative seconds per jlb_evolve phase
     std::string err;
 
     // graphs of GK consecutive steps without moment output, one per parity
     cudaGraphExec_t gexec[2] = {nullptr, nullptr};
     int GK = 32;
+    // bulk-copy staged step (FP32/FP16 on aligned, mostly fluid domains)
+    bool use_tma = false;
+    int tma_grid = 0;
+    int *d_err = nullptr; // set by a kernel whose bounded wait timed out
     uint64_t args_version = 1, graph_version[2] = {0, 0};
 };
 
@@ -499,7 +507,15 @@ int upload_tables(jlb_solver *s) {
         CK(cudaMemcpyAsync(s->d_sp_lw, s->sp_lw.data(), 19 * (size_t)M * sizeof(double), cudaMemcpyHostToDevice, s->st));
     }
     CK(cudaMemcpyAsync(s->nmask, s->hmask.data(), (size_t)s->Np * sizeof(uint32_t), cudaMemcpyHostToDevice, s->st));
-    s->h2d_bytes += (uint64_t)s->Np * sizeof(uint32_t) + (uint64_t)M * (8 + 4 + 3 * 19 * 8);
+    s->hcls.resize((size_t)s->Np);
+#pragma omp parallel for schedule(static)
+    for (int64_t n = 0; n < s->Np; ++n) {
+        const uint32_t m = s->hmask[n];
+        s->hcls[n] = (m & MASK_SOLID) ? CLS_SOLID : (m & MASK_SPECIAL) ? CLS_SPECIAL
+                                                  : (m & MASK_LINKS) ? CLS_WALL : CLS_PLAIN;
+    }
+    CK(cudaMemcpyAsync(s->ncls, s->hcls.data(), (size_t)s->Np, cudaMemcpyHostToDevice, s->st));
+    s->h2d_bytes += (uint64_t)s->Np * 5 + (uint64_t)M * (8 + 4 + 3 * 19 * 8);
     CK(cudaStreamSynchronize(s->st)); // host vectors may be rebuilt right after
     ++s->args_version;
     return JLB_OK;
@@ -535,6 +551,7 @@ StepArgs make_args(const jlb_solver *s, int write_moments) {
     a.Np = s->Np;
     a.nx = s->nx; a.ny = s->ny; a.nz = s->nz;
     a.nmask = s->nmask;
+    a.ncls = s->ncls;
     a.den = s->mom[0]; a.ux = s->mom[1]; a.uy = s->mom[2]; a.uz = s->mom[3];
     a.acc = s->accf ? s->acc : nullptr;
     for (int d = 0; d < 3; ++d) a.g[d] = s->g[d];
@@ -557,12 +574,54 @@ StepArgs make_args(const jlb_solver *s, int write_moments) {
 
 int launch_one(jlb_solver *s, const StepArgs &a, bool pstep) {
     const int blocks = a.nb_dense + (a.M + 127) / 128;
+    const int nsb = (a.M + 127) / 128;
     int r;
-    if (s->prec == PREC_FP64) r = launch_step_fp64(a, s->cfg.rlx_scheme, pstep, s->accf, blocks, s->st);
+    if (s->use_tma) {
+        const int ntiles = a.nb_dense; // one 128-site tile per dense block (bx = 128, by = 1)
+        if (s->prec == PREC_FP32)
+            r = launch_step_tma_fp32(a, s->cfg.rlx_scheme, pstep, s->accf, s->tma_grid, ntiles, nsb, s->d_err, s->st);
+        else
+            r = launch_step_tma_fp16(a, s->cfg.rlx_scheme, pstep, s->accf, s->tma_grid, ntiles, nsb, s->d_err, s->st);
+    } else if (s->prec == PREC_FP64) r = launch_step_fp64(a, s->cfg.rlx_scheme, pstep, s->accf, blocks, s->st);
     else if (s->prec == PREC_FP32) r = launch_step_fp32(a, s->cfg.rlx_scheme, pstep, s->accf, blocks, s->st);
     else r = launch_step_fp16(a, s->cfg.rlx_scheme, pstep, s->accf, blocks, s->st);
     if (r) return fail(s, JLB_ERR_CUDA, std::string("step launch: ") + cudaGetErrorString((cudaError_t)r));
     ++s->launches;
+    return JLB_OK;
+}
+
+// The staged kernel needs 16-byte aligned rows (nz a multiple of 16 bytes of
+// elements), at least one full 128-site tile per row and 32-bit element
+// indices; it only makes sense when most staged sites are fluid.  It is
+// opt-in (JLB_TMA=1): on the 256^3 cavity it measured 71% of HBM against 79%
+// for the direct kernel.
+void choose_kernel(jlb_solver *s) {
+    s->use_tma = false;
+    const char *e = std::getenv("JLB_TMA");
+    if (!e || e[0] != '1') return;
+    if (s->prec == PREC_FP64) return;
+    const int pad = (int)(16 / s->ssz);
+    if (s->nz < 128 || s->nz % pad != 0 || s->Np * 19 > 0x7fffffffLL) return;
+    if ((double)s->nfluid < 0.85 * (double)s->N) return;
+    const int per_sm = s->prec == PREC_FP32 ? tma_blocks_per_sm_fp32(s->cfg.rlx_scheme)
+                                            : tma_blocks_per_sm_fp16(s->cfg.rlx_scheme);
+    int dev = 0, sms = 0;
+    if (per_sm <= 0 || cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) {
+        cudaGetLastError();
+        return;
+    }
+    s->tma_grid = per_sm * sms;
+    s->use_tma = true;
+    ++s->args_version;
+}
+
+// reports a kernel-side timeout recorded in d_err
+int check_kernel_error(jlb_solver *s) {
+    int h = 0;
+    CK(cudaMemcpyAsync(&h, s->d_err, sizeof(int), cudaMemcpyDeviceToHost, s->st));
+    CK(cudaStreamSynchronize(s->st));
+    if (h) return fail(s, JLB_ERR_CUDA, "a step kernel's bounded wait on its bulk copies timed out");
     return JLB_OK;
 }
 
@@ -749,11 +808,17 @@ int jlb_create(const jlb_config *cfg, jlb_solver **out) {
     };
     if ((r = alloc(&s->f, (size_t)19 * s->Np * s->ssz))) return bail(r);
     if ((r = alloc((void **)&s->nmask, (size_t)s->Np * sizeof(uint32_t)))) return bail(r);
+    if ((r = alloc((void **)&s->ncls, (size_t)s->Np))) return bail(r);
     for (int c = 0; c < 4; ++c)
         if ((r = alloc(&s->mom[c], (size_t)s->Np * s->csz))) return bail(r);
     s->red_blocks = aux_reduce_blocks(s->N);
     if ((r = alloc((void **)&s->red_partial, (size_t)8 * s->red_blocks * sizeof(double)))) return bail(r);
     if ((r = alloc((void **)&s->red_out, 8 * sizeof(double)))) return bail(r);
+    if ((r = alloc((void **)&s->d_err, sizeof(int)))) return bail(r);
+    if (cudaMemset(s->d_err, 0, sizeof(int)) != cudaSuccess) {
+        s->err = "cudaMemset failed";
+        return bail(JLB_ERR_CUDA);
+    }
     *out = s;
     return JLB_OK;
 }
@@ -762,9 +827,9 @@ void jlb_destroy(jlb_solver *s) {
     if (!s) return;
     if (s->st) cudaStreamSynchronize(s->st);
     drop_graphs(s);
-    void *bufs[] = {s->f, s->nmask, s->mom[0], s->mom[1], s->mom[2], s->mom[3], s->acc, s->red_partial,
+    void *bufs[] = {s->f, s->nmask, s->ncls, s->mom[0], s->mom[1], s->mom[2], s->mom[3], s->acc, s->red_partial,
                     s->red_out, s->d_sp_node, s->d_sp_info, s->d_sp_rd, s->d_sp_wr, s->d_sp_lw, s->d_sp_bc,
-                    s->d_sp_den};
+                    s->d_sp_den, s->d_err};
     for (void *p : bufs)
         if (p) cudaFree(p);
     if (s->pinned) cudaFreeHost(s->pinned);
@@ -814,6 +879,7 @@ int jlb_finalize_init(jlb_solver *s, uint8_t *phase, double *den, double *vel, u
         cudaFree(dph); cudaFree(dden); cudaFree(dvel);
         if (r) return fail(s, JLB_ERR_CUDA, std::string("init kernel: ") + cudaGetErrorString((cudaError_t)r));
         CK(es);
+        choose_kernel(s);
     } else {
         s->nfluid = 0;
     }
@@ -840,6 +906,9 @@ int jlb_evolve(jlb_solver *s, uint32_t tsteps, const double g[3], double *den, d
         if (tot) *tot = s->tot;
         return JLB_OK;
     }
+    using clk = std::chrono::steady_clock;
+    auto since = [](clk::time_point a) { return std::chrono::duration<double>(clk::now() - a).count(); };
+    const auto t_start = clk::now();
     enforce_den_vel(s, den, vel);
     // solid velocities: reclassify when any of them changed since the last call
     bool changed = false;
@@ -852,8 +921,12 @@ int jlb_evolve(jlb_solver *s, uint32_t tsteps, const double g[3], double *den, d
         int r = upload_tables(s);
         if (r) return r;
     }
+    s->host_t[0] += since(t_start);
+    auto t1 = clk::now();
     fill_dynamic(s, den, vel);
     int r = upload_dynamic(s);
+    s->host_t[1] += since(t1);
+    t1 = clk::now();
     if (r) return r;
     // acceleration field (read every step by the reference, jyulb/isothermal.pyx:1293-1295)
     bool accf = false;
@@ -883,10 +956,17 @@ int jlb_evolve(jlb_solver *s, uint32_t tsteps, const double g[3], double *den, d
         ++s->launches;
     }
     if (accf != s->accf) { s->accf = accf; ++s->args_version; }
+    s->host_t[2] += since(t1);
+    t1 = clk::now();
     r = run_steps(s, tsteps, true);
     if (r) return r;
+    s->host_t[3] += since(t1);
+    t1 = clk::now();
     r = download(s, den, vel);
     if (r) return r;
+    if (s->use_tma && (r = check_kernel_error(s))) return r;
+    s->host_t[4] += since(t1);
+    s->host_t[5] += since(t_start);
     s->tot += tsteps;
     if (tot) *tot = s->tot;
     return JLB_OK;
@@ -960,6 +1040,11 @@ void jlb_rlx_prm(const jlb_solver *s, double out[2]) {
 }
 
 uint64_t jlb_kernel_launches(const jlb_solver *s) { return s ? s->launches : 0; }
+
+void jlb_host_timers(const jlb_solver *s, double out[6]) {
+    if (!out) return;
+    for (int k = 0; k < 6; ++k) out[k] = s ? s->host_t[k] : 0.0;
+}
 
 void jlb_transfer_bytes(const jlb_solver *s, uint64_t out[2]) {
     if (!out) return;

@@ -100,8 +100,10 @@ __device__ __forceinline__ void dense_node(const StepArgs &a, int b) {
     if (row >= a.nx * a.ny || k >= a.nz) return;
     // element indices fit IT (int32 when 19 * Np < 2^31, chosen by the host)
     const IT n = (IT)row * a.nz + k;
-    const uint32_t m = __ldg(a.nmask + n);
-    if (m & MASK_SKIP) return;
+    const uint8_t cls = __ldg(a.ncls + n);
+    if (cls >= CLS_SPECIAL) return;
+    // the link mask matters only to the pull-push step of wall nodes
+    const uint32_t m = (PSTEP && cls == CLS_WALL) ? __ldg(a.nmask + n) : 0u;
 
     S *__restrict__ f = (S *)a.f;
     const IT Np = (IT)a.Np;

@@ -24,7 +24,8 @@ JLB_ERR_NUMERIC = -6
 EXPORTED_SYMBOLS = (
     "jlb_check_config", "jlb_create", "jlb_destroy", "jlb_finalize_init", "jlb_evolve",
     "jlb_step", "jlb_download_moments", "jlb_get_populations", "jlb_set_populations",
-    "jlb_reduce", "jlb_reduce_moments_noalloc", "jlb_tot_tsteps", "jlb_rlx_prm", "jlb_kernel_launches", "jlb_transfer_bytes",
+    "jlb_reduce", "jlb_reduce_moments_noalloc", "jlb_tot_tsteps", "jlb_rlx_prm", "jlb_kernel_launches",
+    "jlb_transfer_bytes", "jlb_host_timers",
     "jlb_last_error",
     "jlb_build_info",
 )
@@ -79,6 +80,7 @@ def load() -> ctypes.CDLL:
         "jlb_rlx_prm": (None, [vp, dp]),
         "jlb_kernel_launches": (ctypes.c_uint64, [vp]),
         "jlb_transfer_bytes": (None, [vp, ctypes.POINTER(ctypes.c_uint64)]),
+        "jlb_host_timers": (None, [vp, dp]),
         "jlb_last_error": (ctypes.c_char_p, [vp]),
         "jlb_build_info": (ctypes.c_char_p, []),
     }
