@@ -86,8 +86,8 @@ struct jlb_solver {
     std::vector<int64_t> sp_node;
     std::vector<uint32_t> sp_info;
     std::vector<int64_t> sp_rd, sp_wr;
-    std::vector<double> sp_lw, sp_bc;
-    std::vector<double> sp_den_h;
+    std::vector<double> sp_lw;
+    int bc_slots = 0;                // Zou-He data sets per boundary node
     void *pinned = nullptr;          // staging for per-call uploads
     size_t pinned_bytes = 0;
 
@@ -107,6 +107,7 @@ struct jlb_solver {
     int GK = 32;
     // bulk-copy staged step (FP32/FP16 on aligned, mostly fluid domains)
     bool use_tma = false;
+    bool tma_p = true; // also for the pull-push step
     int tma_grid = 0;
     int *d_err = nullptr; // set by a kernel whose bounded wait timed out
     uint64_t args_version = 1, graph_version[2] = {0, 0};
@@ -380,9 +381,9 @@ void build_special(jlb_solver *s, const double *vel) {
     s->sp_rd.assign((size_t)19 * M, 0);
     s->sp_wr.assign((size_t)19 * M, 0);
     s->sp_lw.assign((size_t)19 * M, 0.0);
-    s->sp_bc.assign((size_t)8 * M, 0.0);
-    s->sp_den_h.assign(M, 1.0);
     const int64_t Np = s->Np;
+    int slots = 0;
+#pragma omp parallel for schedule(static) reduction(max : slots) if (M > 4096)
     for (int t = 0; t < M; ++t) {
         const int64_t n = s->sp_node[t];
         const int i = (int)(n / ((int64_t)s->ny * s->nz));
@@ -430,23 +431,32 @@ void build_special(jlb_solver *s, const double *vel) {
         }
         // Zou-He faces of this node
         const int at[6] = {i == 0, i == s->nx - 1, j == 0, j == s->ny - 1, k == 0, k == s->nz - 1};
+        int nf = 0;
         for (int face = 0; face < 6; ++face)
-            if (at[face] && is_fixed(bc[face])) info |= 1u << (SP_FACE_SHIFT + face);
+            if (at[face] && is_fixed(bc[face])) { info |= 1u << (SP_FACE_SHIFT + face); ++nf; }
         s->sp_info[t] = info;
+        slots = std::max(slots, nf);
     }
+    s->bc_slots = slots; // Zou-He data sets per boundary node (0, 1 or 2)
 }
 
 // per-call Zou-He data and previous-step density of the boundary nodes
-void fill_dynamic(jlb_solver *s, const double *den, const double *vel) {
+// Per-call inputs of the boundary nodes, written straight into the
+// page-locked staging buffer: Zou-He data (bc_slots x 4 doubles per node,
+// slot-major) followed by the previous-step density in the compute type.
+void fill_dynamic(jlb_solver *s, const double *den, const double *vel, double *bcbuf, void *denbuf) {
     const int M = s->M;
     const int *bc = s->cfg.bc;
+    const bool f64 = s->prec == PREC_FP64;
+#pragma omp parallel for schedule(static) if (M > 4096)
     for (int t = 0; t < M; ++t) {
         const int64_t n = s->sp_node[t];
         const int i = (int)(n / ((int64_t)s->ny * s->nz));
         const int j = (int)((n / s->nz) % s->ny);
         const int k = (int)(n % s->nz);
         const int64_t fn = fidx(s, i + 1, j + 1, k + 1);
-        s->sp_den_h[t] = den[fn];
+        if (f64) ((double *)denbuf)[t] = den[fn];
+        else ((float *)denbuf)[t] = (float)(den[fn] - 1.0);
         const uint32_t faces = (s->sp_info[t] >> SP_FACE_SHIFT) & 0x3Fu;
         int slot = 0;
         for (int face = 0; face < 6 && faces; ++face) {
@@ -458,11 +468,10 @@ void fill_dynamic(jlb_solver *s, const double *den, const double *vel) {
             if (face == 5) refresh = bc[5] == BC_FIXED_DEN || bc[4] == BC_FIXED_VEL;
             double d = 1.0, u0 = 0.0, u1 = 0.0, u2 = 0.0;
             if (refresh) { d = den[fn]; u0 = vel[3 * fn]; u1 = vel[3 * fn + 1]; u2 = vel[3 * fn + 2]; }
-            double *b = s->sp_bc.data();
-            b[(size_t)(4 * slot) * M + t] = d;
-            b[(size_t)(4 * slot + 1) * M + t] = u0;
-            b[(size_t)(4 * slot + 2) * M + t] = u1;
-            b[(size_t)(4 * slot + 3) * M + t] = u2;
+            bcbuf[(size_t)(4 * slot) * M + t] = d;
+            bcbuf[(size_t)(4 * slot + 1) * M + t] = u0;
+            bcbuf[(size_t)(4 * slot + 2) * M + t] = u1;
+            bcbuf[(size_t)(4 * slot + 3) * M + t] = u2;
             slot = 1;
         }
     }
@@ -522,26 +531,19 @@ int upload_tables(jlb_solver *s) {
 }
 
 // uploads bc data and previous-step density of the boundary nodes
-int upload_dynamic(jlb_solver *s) {
+int upload_dynamic(jlb_solver *s, const double *den, const double *vel) {
     const int M = s->M;
     if (M == 0) return JLB_OK;
-    const size_t bc_bytes = 8 * (size_t)M * sizeof(double);
+    const size_t bc_bytes = 4 * (size_t)s->bc_slots * M * sizeof(double);
     const size_t den_bytes = (size_t)M * s->csz;
     int r = ensure_pinned(s, bc_bytes + den_bytes + 64);
     if (r) return r;
     CK(cudaStreamSynchronize(s->st)); // staging buffer may still be in flight
     char *pin = (char *)s->pinned;
-    std::memcpy(pin, s->sp_bc.data(), bc_bytes);
-    char *dp = pin + bc_bytes;
-    if (s->prec == PREC_FP64) {
-        std::memcpy(dp, s->sp_den_h.data(), den_bytes);
-    } else {
-        float *fd = (float *)dp;
-        for (int t = 0; t < M; ++t) fd[t] = (float)(s->sp_den_h[t] - 1.0);
-    }
-    CK(cudaMemcpyAsync(s->d_sp_bc, pin, bc_bytes, cudaMemcpyHostToDevice, s->st));
+    fill_dynamic(s, den, vel, (double *)pin, pin + bc_bytes);
+    if (bc_bytes) CK(cudaMemcpyAsync(s->d_sp_bc, pin, bc_bytes, cudaMemcpyHostToDevice, s->st));
+    CK(cudaMemcpyAsync(s->d_sp_den, pin + bc_bytes, den_bytes, cudaMemcpyHostToDevice, s->st));
     s->h2d_bytes += bc_bytes + den_bytes;
-    CK(cudaMemcpyAsync(s->d_sp_den, dp, den_bytes, cudaMemcpyHostToDevice, s->st));
     return JLB_OK;
 }
 
@@ -576,7 +578,7 @@ int launch_one(jlb_solver *s, const StepArgs &a, bool pstep) {
     const int blocks = a.nb_dense + (a.M + 127) / 128;
     const int nsb = (a.M + 127) / 128;
     int r;
-    if (s->use_tma) {
+    if (s->use_tma && (s->tma_p || !pstep)) {
         const int ntiles = a.nb_dense; // one 128-site tile per dense block (bx = 128, by = 1)
         if (s->prec == PREC_FP32)
             r = launch_step_tma_fp32(a, s->cfg.rlx_scheme, pstep, s->accf, s->tma_grid, ntiles, nsb, s->d_err, s->st);
@@ -592,13 +594,16 @@ int launch_one(jlb_solver *s, const StepArgs &a, bool pstep) {
 
 // The staged kernel needs 16-byte aligned rows (nz a multiple of 16 bytes of
 // elements), at least one full 128-site tile per row and 32-bit element
-// indices; it only makes sense when most staged sites are fluid.  It is
-// opt-in (JLB_TMA=1): on the 256^3 cavity it measured 71% of HBM against 79%
-// for the direct kernel.
+// indices; it only makes sense when most staged sites are fluid.  By default
+// it runs the local (L) step, whose reads are aligned whole rows, and the
+// direct kernel runs the pull-push (P) step: on the 256^3 cavity that split
+// measured 81% of HBM, direct-only 79%, staged-only 74%.  JLB_TMA=0 disables
+// staging, JLB_TMA=1 stages both steps.
 void choose_kernel(jlb_solver *s) {
     s->use_tma = false;
     const char *e = std::getenv("JLB_TMA");
-    if (!e || e[0] != '1') return;
+    if (e && e[0] == '0') return;
+    s->tma_p = e && e[0] == '1';
     if (s->prec == PREC_FP64) return;
     const int pad = (int)(16 / s->ssz);
     if (s->nz < 128 || s->nz % pad != 0 || s->Np * 19 > 0x7fffffffLL) return;
@@ -911,10 +916,12 @@ int jlb_evolve(jlb_solver *s, uint32_t tsteps, const double g[3], double *den, d
     const auto t_start = clk::now();
     enforce_den_vel(s, den, vel);
     // solid velocities: reclassify when any of them changed since the last call
-    bool changed = false;
-    for (size_t w = 0; w < s->wall_pos.size() && !changed; ++w) {
+    int changed = 0;
+    const int64_t nwall = (int64_t)s->wall_pos.size();
+#pragma omp parallel for schedule(static) reduction(| : changed) if (nwall > 16384)
+    for (int64_t w = 0; w < nwall; ++w) {
         const double *u = vel + 3 * s->wall_pos[w];
-        changed = u[0] != s->wall_vel[3 * w] || u[1] != s->wall_vel[3 * w + 1] || u[2] != s->wall_vel[3 * w + 2];
+        changed |= (u[0] != s->wall_vel[3 * w]) | (u[1] != s->wall_vel[3 * w + 1]) | (u[2] != s->wall_vel[3 * w + 2]);
     }
     if (changed) {
         build_special(s, vel);
@@ -923,8 +930,7 @@ int jlb_evolve(jlb_solver *s, uint32_t tsteps, const double g[3], double *den, d
     }
     s->host_t[0] += since(t_start);
     auto t1 = clk::now();
-    fill_dynamic(s, den, vel);
-    int r = upload_dynamic(s);
+    int r = upload_dynamic(s, den, vel);
     s->host_t[1] += since(t1);
     t1 = clk::now();
     if (r) return r;

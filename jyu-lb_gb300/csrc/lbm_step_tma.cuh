@@ -167,21 +167,27 @@ __global__ void __launch_bounds__(128, JLB_MIN_BLOCKS) lbm_step_tma_kernel(const
                 dJ[0] = (j == 0 ? (a.ny - 1) : -1) * sJ; dJ[1] = 0; dJ[2] = (j + 1 == a.ny ? (1 - a.ny) : 1) * sJ;
                 dK[0] = k == 0 ? (a.nz - 1) : -1; dK[1] = 0; dK[2] = k + 1 == a.nz ? (1 - a.nz) : 1;
             }
+            // every lane takes its value from the staged rows (the index stays
+            // inside the slot's segment even where it is not the right value)
             Unroll<0, Q>::run([&]<int q>() {
-                if (!PSTEP || q == 9) {
-                    fv[q] = ST::template ldv<q>(cur[q * G::SEG + G::PAD + t]);
-                } else {
+                constexpr int sh = (PSTEP && q != 9) ? CZ(q) : 0;
+                fv[q] = ST::template ldv<q>(cur[q * G::SEG + G::PAD + t - sh]);
+            });
+            // rare lanes fix theirs up from global memory: links that bounce
+            // back read their own opposite slot; sources that wrap in k
+            // (periodic) lie outside the staged window
+            if (PSTEP && (m != 0u || k == 0 || k == a.nz - 1)) {
+                Unroll<0, Q>::run([&]<int q>() {
+                    if (q == 9) return;
                     const int kk = k - CZ(q);
                     if (m & (1u << q)) {
                         fv[q] = ST::template ld<q>(f + ((int32_t)q * Np + n));
                     } else if (kk < 0 || kk >= a.nz) {
                         const int32_t src = n + dI[1 - CX(q)] + dJ[1 - CY(q)] + dK[1 - CZ(q)];
                         fv[q] = ST::template ld<q>(f + ((int32_t)OPP(q) * Np + src));
-                    } else {
-                        fv[q] = ST::template ldv<q>(cur[q * G::SEG + G::PAD + t - CZ(q)]);
                     }
-                }
-            });
+                });
+            }
             C ax, ay, az;
             if (ACCF) {
                 const C *acc = (const C *)a.acc;
