@@ -140,6 +140,45 @@ int jlb_reduce(jlb_solver *s, double out[8]);
 int jlb_reduce_moments_noalloc(const uint32_t *nmask, const void *den, const void *ux, const void *uy,
                                const void *uz, int64_t n_sites, int32_t precision, double *out, void *stream);
 
+/* ---------------------------------------------------------------------
+ * Batched ensemble: many independent domains advanced by one launch per
+ * step over a packed node index.  The reference advances one Solver at a
+ * time (jyulb/isothermal.pyx:1370-1418); an ensemble of its channels is a
+ * loop over Solver objects, which these calls replace.  Populations are
+ * FP32 shifted; faces may be WALL or PERIODIC; solids that move must share
+ * one velocity per domain (Ladd's term, jyulb/isothermal.pyx:1117-1119).
+ * --------------------------------------------------------------------- */
+typedef struct jlb_batch jlb_batch;
+
+typedef struct jlb_domain {
+    int32_t lat_size[3];  /* interior sites per axis                         */
+    double kvisc;         /* kinematic viscosity                             */
+    double g[3];          /* body force                                      */
+    int32_t bc[6];        /* JLB_WALL / JLB_PERIODIC per face                 */
+    double trt_magic;     /* as in jlb_config                                */
+    const uint8_t *phase; /* (nx,ny,nz) interior phase, k fastest, 0 = solid */
+    const double *den;    /* (nx,ny,nz) initial density or NULL (1)          */
+    const double *vel;    /* (nx,ny,nz,3) initial velocity / solid velocity, or NULL */
+} jlb_domain;
+
+/* Sets up all domains (the single-domain halo rules, masks and initial
+ * populations of each, jyulb/isothermal.pyx:1333-1365) and picks the block
+ * size with a timing autotuner (JLB_BATCH_BLOCK=64/128/256 fixes it). */
+int jlb_batch_create(int32_t rlx_scheme, const jlb_domain *doms, int32_t ndom, void *stream, jlb_batch **out);
+void jlb_batch_destroy(jlb_batch *b);
+/* advances every domain tsteps steps (one launch per step, graph-replayed);
+ * moments of the last step are stored */
+int jlb_batch_step(jlb_batch *b, uint32_t tsteps);
+/* den (nx,ny,nz) and vel (nx,ny,nz,3) of domain d on its fluid sites */
+int jlb_batch_moments(jlb_batch *b, int32_t d, double *den, double *vel);
+/* post-collision populations of domain d, (19, nx, ny, nz) FP64 */
+int jlb_batch_populations(jlb_batch *b, int32_t d, double *f);
+/* out: total packed sites, fluid sites, block size, tiles, launches, and the
+ * autotuner's per-step times (ns) for blocks of 64, 128, 256 */
+int jlb_batch_info(const jlb_batch *b, int64_t out[8]);
+int32_t jlb_batch_domain_fluid(const jlb_batch *b, int32_t d);
+const char *jlb_batch_last_error(const jlb_batch *b);
+
 /* number of steps taken since finalize (Solver.tot_tsteps) */
 uint32_t jlb_tot_tsteps(const jlb_solver *s);
 

@@ -1,0 +1,160 @@
+// lbm_batch.cu -- one launch advances many independent D3Q19 domains.
+//
+// The domains' nodes are packed into one index space (each domain starts at
+// a multiple of 128), populations are stored SoA over that space in FP32 as
+// f - w (the shifted storage of lbm_fp32.cu), and the launch walks a tile
+// table: tile t covers BLOCK consecutive nodes of domain tile_dom[t].  Per
+// domain the kernel reads its relaxation rates, body force, sizes (for the
+// periodic wrap) and the velocity of its moving solids.  Supported
+// boundaries are those of a channel ensemble: periodic faces, bounce-back
+// walls and solids (node link masks), and Ladd's moving-wall term for solids
+// that move with the domain's wall velocity.  The AA pair and the physics
+// are the single-domain kernels' (lbm_step.cuh, lbm_shifted.cuh).
+#include "lbm_batch.h"
+#include "lbm_shifted.cuh"
+
+namespace jlb {
+
+template <int SCH, bool PSTEP, int BLOCK>
+__global__ void __launch_bounds__(BLOCK, (BLOCK >= 256 ? 3 : BLOCK >= 128 ? 6 : 12))
+    lbm_batch_kernel(const BatchArgs a) {
+    using ST = StoreF32;
+    using PH = PhysSh<SCH>;
+    using C = float;
+    const int t = (int)blockIdx.x;
+    const int d = __ldg(a.tile_dom + t);
+    const BatchDomain &D = a.dom[d];
+    const int32_t l = (t - D.first_tile) * BLOCK + (int)threadIdx.x;
+    if (l >= D.n) return;
+    const int32_t n = D.off + l;
+    const uint8_t cls = __ldg(a.ncls + n);
+    if (cls == BCLS_SOLID) return;
+    const int64_t Np = a.Np; // 19 * Np exceeds 2^31 for large ensembles
+    float *__restrict__ f = a.f;
+    const uint32_t m = (PSTEP && cls != BCLS_PLAIN) ? __ldg(a.nmask + n) : 0u;
+    const uint32_t mv = (cls == BCLS_MOVING) ? __ldg(a.mmask + n) : 0u;
+    C fv[Q];
+    int32_t dI[3], dJ[3], dK[3];
+    if (PSTEP) {
+        const int32_t syz = D.ny * D.nz;
+        const int i = l / syz;
+        const int r = l - i * syz;
+        const int j = r / D.nz;
+        const int k = r - j * D.nz;
+        dI[0] = (i == 0 ? (D.nx - 1) : -1) * syz; dI[1] = 0; dI[2] = (i + 1 == D.nx ? (1 - D.nx) : 1) * syz;
+        dJ[0] = (j == 0 ? (D.ny - 1) : -1) * D.nz; dJ[1] = 0; dJ[2] = (j + 1 == D.ny ? (1 - D.ny) : 1) * D.nz;
+        dK[0] = k == 0 ? (D.nz - 1) : -1; dK[1] = 0; dK[2] = k + 1 == D.nz ? (1 - D.nz) : 1;
+    }
+    Unroll<0, Q>::run([&]<int q>() {
+        int64_t e;
+        if (!PSTEP || q == 9) {
+            e = (int64_t)q * Np + n;
+        } else {
+            const int32_t src = n + dI[1 - CX(q)] + dJ[1 - CY(q)] + dK[1 - CZ(q)];
+            e = (m & (1u << q)) ? ((int64_t)q * Np + n) : ((int64_t)OPP(q) * Np + src);
+        }
+        fv[q] = ST::template ld<q>(f + e);
+    });
+    if (mv) {
+        // Ladd's term on links to moving solids: 6 w_q rho_prev (c_q . U)
+        const float dprev = a.dprev[n];
+        Unroll<0, Q>::run([&]<int q>() {
+            if (q == 9 || !(mv & (1u << q))) return;
+            constexpr int cx = CX(q), cy = CY(q), cz = CZ(q);
+            const float s = (float)cx * D.uw[0] + (float)cy * D.uw[1] + (float)cz * D.uw[2];
+            fv[q] = PH::template ladd<q>(fv[q], dprev, s);
+        });
+    }
+    C ux, uy, uz;
+    const C dd = PH::collide(fv, D.g[0], D.g[1], D.g[2], D.we, D.wo, ux, uy, uz);
+    Unroll<0, Q>::run([&]<int q>() {
+        if (!PSTEP) {
+            ST::template st<OPP(q)>(f + ((int64_t)OPP(q) * Np + n), fv[q]);
+            return;
+        }
+        int64_t e;
+        if (q == 9) {
+            e = 9 * Np + n;
+        } else {
+            const int32_t dst = n + dI[1 + CX(q)] + dJ[1 + CY(q)] + dK[1 + CZ(q)];
+            e = (m & (1u << OPP(q))) ? ((int64_t)OPP(q) * Np + n) : ((int64_t)q * Np + dst);
+        }
+        ST::template st<q>(f + e, fv[q]);
+    });
+    if (mv) a.dprev[n] = dd;
+    if (a.write_moments) {
+        a.den[n] = dd;
+        a.ux[n] = ux;
+        a.uy[n] = uy;
+        a.uz[n] = uz;
+    }
+}
+
+int launch_batch_step(const BatchArgs &a, int scheme, bool pstep, int block, int ntiles, cudaStream_t st) {
+#define JLB_B(SCH, P, B) lbm_batch_kernel<SCH, P, B><<<ntiles, B, 0, st>>>(a)
+#define JLB_BB(SCH, B) if (pstep) JLB_B(SCH, true, B); else JLB_B(SCH, false, B);
+#define JLB_BS(SCH)                               \
+    if (block == 64) { JLB_BB(SCH, 64) }          \
+    else if (block == 256) { JLB_BB(SCH, 256) }   \
+    else { JLB_BB(SCH, 128) }
+    if (scheme == SCH_BGK) { JLB_BS(SCH_BGK) }
+    else if (scheme == SCH_TRT) { JLB_BS(SCH_TRT) }
+    else { JLB_BS(SCH_REG) }
+#undef JLB_BS
+#undef JLB_BB
+#undef JLB_B
+    return (int)cudaGetLastError();
+}
+
+// gathers one domain's initial populations (single-domain S_post layout,
+// stride Np_d) into the packed array (stride Np)
+__global__ void batch_pack_kernel(const float *src, int64_t Np_d, int32_t n_d, float *dst, int64_t Np,
+                                  int32_t off) {
+    const int32_t l = blockIdx.x * blockDim.x + threadIdx.x;
+    if (l >= n_d) return;
+#pragma unroll
+    for (int q = 0; q < Q; ++q) dst[(int64_t)q * Np + off + l] = src[(int64_t)q * Np_d + l];
+}
+
+int launch_batch_pack(const float *src, int64_t Np_d, int32_t n_d, float *dst, int64_t Np, int32_t off,
+                      cudaStream_t st) {
+    batch_pack_kernel<<<(n_d + 255) / 256, 256, 0, st>>>(src, Np_d, n_d, dst, Np, off);
+    return (int)cudaGetLastError();
+}
+
+// post-collision populations of one domain (any parity) as FP64 (19, n_d)
+__global__ void batch_readout_kernel(BatchArgs a, int d, int parity, double *out) {
+    const BatchDomain &D = a.dom[d];
+    const int32_t l = blockIdx.x * blockDim.x + threadIdx.x;
+    if (l >= D.n) return;
+    const int32_t n = D.off + l;
+    const uint8_t cls = a.ncls[n];
+    if (cls == BCLS_SOLID) {
+        for (int q = 0; q < Q; ++q) out[(int64_t)q * D.n + l] = 0.0;
+        return;
+    }
+    const uint32_t m = cls != BCLS_PLAIN ? a.nmask[n] : 0u;
+    const int32_t syz = D.ny * D.nz;
+    const int i = l / syz, r = l - (l / syz) * syz, j = r / D.nz, k = r - (r / D.nz) * D.nz;
+    Unroll<0, Q>::run([&]<int q>() {
+        constexpr double w = WCLASS(q) == 0 ? (12.0 / 36.0) : WCLASS(q) == 1 ? (2.0 / 36.0) : (1.0 / 36.0);
+        int64_t e;
+        if (parity == 0 || q == 9 || (m & (1u << OPP(q)))) {
+            e = (int64_t)OPP(q) * a.Np + n;
+        } else {
+            int ii = i + CX(q), jj = j + CY(q), kk = k + CZ(q);
+            ii = ii < 0 ? D.nx - 1 : (ii >= D.nx ? 0 : ii);
+            jj = jj < 0 ? D.ny - 1 : (jj >= D.ny ? 0 : jj);
+            kk = kk < 0 ? D.nz - 1 : (kk >= D.nz ? 0 : kk);
+            e = (int64_t)q * a.Np + D.off + (ii * D.ny + jj) * D.nz + kk;
+        }
+        out[(int64_t)q * D.n + l] = (double)a.f[e] + w;
+    });
+}
+
+int launch_batch_readout(const BatchArgs &a, int d, int n_d, int parity, double *out, cudaStream_t st) {
+    batch_readout_kernel<<<(n_d + 255) / 256, 256, 0, st>>>(a, d, parity, out);
+    return (int)cudaGetLastError();
+}
+
+} // namespace jlb

@@ -1,0 +1,44 @@
+// lbm_batch.h -- device-side description of a batched ensemble of domains
+// (lbm_batch.cu) and its launchers.
+#pragma once
+#include <stdint.h>
+#include <cuda_runtime.h>
+#include "lbm_common.h"
+
+namespace jlb {
+
+// node classes of the packed ensemble (uint8 per node)
+constexpr uint8_t BCLS_PLAIN = 0;  // fluid, no bounce-back link
+constexpr uint8_t BCLS_WALL = 1;   // fluid with bounce-back links to resting solids
+constexpr uint8_t BCLS_MOVING = 2; // fluid with links to moving solids (Ladd)
+constexpr uint8_t BCLS_SOLID = 3;  // not a fluid node
+
+struct BatchDomain {
+    int32_t off;        // first packed node (multiple of 128)
+    int32_t n;          // nx * ny * nz
+    int32_t nx, ny, nz;
+    int32_t first_tile; // first tile of this domain in the tile table
+    float we, wo;       // relaxation rates
+    float g[3];         // body force
+    float uw[3];        // velocity of the domain's moving solids
+};
+
+struct BatchArgs {
+    float *f;              // 19 * Np, f - w
+    int64_t Np;            // slot stride (multiple of 128)
+    const BatchDomain *dom;
+    const int32_t *tile_dom;
+    const uint8_t *ncls;
+    const uint32_t *nmask; // bounce-back links (WALL / MOVING nodes)
+    const uint32_t *mmask; // links whose source moves (MOVING nodes)
+    float *dprev;          // previous-step rho - 1 (MOVING nodes)
+    float *den, *ux, *uy, *uz;
+    int write_moments;
+};
+
+int launch_batch_step(const BatchArgs &a, int scheme, bool pstep, int block, int ntiles, cudaStream_t st);
+int launch_batch_pack(const float *src, int64_t Np_d, int32_t n_d, float *dst, int64_t Np, int32_t off,
+                      cudaStream_t st);
+int launch_batch_readout(const BatchArgs &a, int d, int n_d, int parity, double *out, cudaStream_t st);
+
+} // namespace jlb

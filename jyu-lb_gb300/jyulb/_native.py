@@ -26,7 +26,8 @@ EXPORTED_SYMBOLS = (
     "jlb_step", "jlb_download_moments", "jlb_get_populations", "jlb_set_populations",
     "jlb_reduce", "jlb_reduce_moments_noalloc", "jlb_tot_tsteps", "jlb_rlx_prm", "jlb_kernel_launches",
     "jlb_transfer_bytes", "jlb_host_timers",
-    "jlb_last_error",
+    "jlb_last_error", "jlb_batch_create", "jlb_batch_destroy", "jlb_batch_step", "jlb_batch_moments",
+    "jlb_batch_populations", "jlb_batch_info", "jlb_batch_domain_fluid", "jlb_batch_last_error",
     "jlb_build_info",
 )
 
@@ -41,6 +42,19 @@ class jlb_config(ctypes.Structure):
         ("precision", ctypes.c_int32),
         ("trt_magic", ctypes.c_double),
         ("stream", ctypes.c_void_p),
+    ]
+
+
+class jlb_domain(ctypes.Structure):
+    _fields_ = [
+        ("lat_size", ctypes.c_int32 * 3),
+        ("kvisc", ctypes.c_double),
+        ("g", ctypes.c_double * 3),
+        ("bc", ctypes.c_int32 * 6),
+        ("trt_magic", ctypes.c_double),
+        ("phase", ctypes.POINTER(ctypes.c_uint8)),
+        ("den", ctypes.POINTER(ctypes.c_double)),
+        ("vel", ctypes.POINTER(ctypes.c_double)),
     ]
 
 
@@ -82,6 +96,15 @@ def load() -> ctypes.CDLL:
         "jlb_transfer_bytes": (None, [vp, ctypes.POINTER(ctypes.c_uint64)]),
         "jlb_host_timers": (None, [vp, dp]),
         "jlb_last_error": (ctypes.c_char_p, [vp]),
+        "jlb_batch_create": (ctypes.c_int, [ctypes.c_int32, ctypes.POINTER(jlb_domain), ctypes.c_int32, vp,
+                                            ctypes.POINTER(vp)]),
+        "jlb_batch_destroy": (None, [vp]),
+        "jlb_batch_step": (ctypes.c_int, [vp, ctypes.c_uint32]),
+        "jlb_batch_moments": (ctypes.c_int, [vp, ctypes.c_int32, dp, dp]),
+        "jlb_batch_populations": (ctypes.c_int, [vp, ctypes.c_int32, dp]),
+        "jlb_batch_info": (ctypes.c_int, [vp, ctypes.POINTER(ctypes.c_int64)]),
+        "jlb_batch_domain_fluid": (ctypes.c_int32, [vp, ctypes.c_int32]),
+        "jlb_batch_last_error": (ctypes.c_char_p, [vp]),
         "jlb_build_info": (ctypes.c_char_p, []),
     }
     for name, (res, args) in sig.items():
