@@ -179,6 +179,29 @@ int jlb_batch_info(const jlb_batch *b, int64_t out[8]);
 int32_t jlb_batch_domain_fluid(const jlb_batch *b, int32_t d);
 const char *jlb_batch_last_error(const jlb_batch *b);
 
+/* ---------------------------------------------------------------------
+ * Discrete adjoint of the time step (no counterpart in the reference, which
+ * has no derivatives).  A problem is a domain described by a jlb_config:
+ * BGK or TRT, FP64 or FP32, started from rest; its parameters are the relaxation time
+ * tau, the body force g and the u_x of each site of a FIXED_VEL face 1X.
+ * The loss is sum |u - target|^2 of the stored velocity on the plane
+ * x = loss_plane after the last step.  The forward run keeps checkpoints
+ * every checkpoint_every steps; the backward run recomputes each segment and
+ * sweeps the adjoint step back through it.
+ * --------------------------------------------------------------------- */
+typedef struct jlb_adjoint jlb_adjoint;
+
+int jlb_adj_create(const jlb_config *cfg, const uint8_t *phase, int32_t loss_plane, int32_t checkpoint_every,
+                   jlb_adjoint **out);
+void jlb_adj_destroy(jlb_adjoint *a);
+/* uin: (ny,nz) inlet u_x; target: (ny,nz,3) or NULL; u_plane: (ny,nz,3) out
+ * or NULL; rho_out: density of FIXED_DEN faces */
+int jlb_adj_forward(jlb_adjoint *a, double tau, const double g[3], const double *uin, double rho_out,
+                    uint32_t steps, const double *target, double *loss, double *u_plane);
+/* gradients of the last forward run's loss; duin: (ny,nz) */
+int jlb_adj_backward(jlb_adjoint *a, double *dtau, double dg[3], double *duin);
+const char *jlb_adj_last_error(const jlb_adjoint *a);
+
 /* number of steps taken since finalize (Solver.tot_tsteps) */
 uint32_t jlb_tot_tsteps(const jlb_solver *s);
 

@@ -30,11 +30,12 @@ UNITS = {
     "lbm_aux.cu": ["-fmad=false"],
     "lbm_noalloc.cu": [],
     "lbm_batch.cu": [],
+    "lbm_adjoint.cu": [],
     # host arithmetic (relaxation rates, Ladd projections) must not be
     # FMA-contracted either: gcc contracts by default on aarch64
     "lbm_host.cpp": ["-x", "cu", "-Xcompiler", "-fopenmp", "-Xcompiler", "-ffp-contract=off"],
 }
-HEADERS = ["lbm_common.h", "lbm_step.cuh", "lbm_step_tma.cuh", "lbm_shifted.cuh", "lbm_aux.h", "lbm_batch.h"]
+HEADERS = ["lbm_common.h", "lbm_step.cuh", "lbm_step_tma.cuh", "lbm_shifted.cuh", "lbm_aux.h", "lbm_batch.h", "lbm_adjoint.h"]
 
 
 def _nvcc() -> str:

@@ -69,6 +69,8 @@ struct StepArgs {
     const double *sp_bc;  // [8][M] Zou-He data (den, ux, uy, uz) x 2 faces
     void *sp_den;         // [M] previous-step density (compute type; rho-1 if shifted)
     int bc[6];            // face kinds (for the Zou-He variant)
+    void *tee;            // if set: collision inputs (after Zou-He) of every
+                          // fluid node, [19][Np] in the storage type (adjoint recompute)
 };
 
 // launch entry points, one per precision translation unit

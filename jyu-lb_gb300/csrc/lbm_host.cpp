@@ -110,6 +110,7 @@ struct jlb_solver {
     bool tma_p = true; // also for the pull-push step
     int tma_grid = 0;
     int *d_err = nullptr; // set by a kernel whose bounded wait timed out
+    void *tee = nullptr;  // adjoint recompute: where steps copy their collision inputs
     uint64_t args_version = 1, graph_version[2] = {0, 0};
 };
 
@@ -570,6 +571,7 @@ StepArgs make_args(const jlb_solver *s, int write_moments) {
     a.sp_rd = s->d_sp_rd; a.sp_wr = s->d_sp_wr;
     a.sp_lw = s->d_sp_lw; a.sp_bc = s->d_sp_bc;
     a.sp_den = s->d_sp_den;
+    a.tee = s->tee;
     for (int f = 0; f < 6; ++f) a.bc[f] = s->cfg.bc[f];
     return a;
 }
@@ -578,7 +580,7 @@ int launch_one(jlb_solver *s, const StepArgs &a, bool pstep) {
     const int blocks = a.nb_dense + (a.M + 127) / 128;
     const int nsb = (a.M + 127) / 128;
     int r;
-    if (s->use_tma && (s->tma_p || !pstep)) {
+    if (s->use_tma && !s->tee && (s->tma_p || !pstep)) {
         const int ntiles = a.nb_dense; // one 128-site tile per dense block (bx = 128, by = 1)
         if (s->prec == PREC_FP32)
             r = launch_step_tma_fp32(a, s->cfg.rlx_scheme, pstep, s->accf, s->tma_grid, ntiles, nsb, s->d_err, s->st);
@@ -1489,5 +1491,271 @@ int32_t jlb_batch_domain_fluid(const jlb_batch *b, int32_t d) {
 }
 
 const char *jlb_batch_last_error(const jlb_batch *b) { return b ? b->err.c_str() : g_create_error.c_str(); }
+
+} // extern "C"
+
+// ===========================================================================
+// Adjoint of the time step with checkpointing (lbm_adjoint.cu)
+// ===========================================================================
+#include "lbm_adjoint.h"
+
+struct jlb_adjoint {
+    jlb_solver *s = nullptr;
+    int K = 50;               // checkpoint interval
+    int plane = 0;
+    double magic = 0.0;       // TRT magic parameter (<= 0: reference's 3/16)
+    void *f0 = nullptr;       // initial populations
+    std::vector<void *> ckpt; // populations before steps 0, K, 2K, ...
+    std::vector<void *> tee;  // collision inputs of the K steps of a segment
+    void *lam = nullptr;
+    double *d_target = nullptr, *d_grad = nullptr, *d_guin = nullptr;
+    uint32_t steps = 0;
+    double tau = 1.0;
+    bool have_forward = false;
+    size_t fbytes = 0;
+    std::string err;
+};
+
+namespace {
+
+int afail(jlb_adjoint *A, int code, const std::string &m) {
+    if (A) A->err = m;
+    else g_create_error = m;
+    return code;
+}
+
+#define ACK(call)                                                                                  \
+    do {                                                                                           \
+        cudaError_t e_ = (call);                                                                   \
+        if (e_ != cudaSuccess)                                                                     \
+            return afail(A, e_ == cudaErrorMemoryAllocation ? JLB_ERR_NOMEM : JLB_ERR_CUDA,        \
+                         std::string(#call) + ": " + cudaGetErrorString(e_));                      \
+    } while (0)
+
+// relaxation rates of relaxation time tau (jyulb/isothermal.pyx:274-287)
+void adj_rates(const jlb_adjoint *A, double tau, double &we, double &wo) {
+    we = 1.0 / tau;
+    wo = we;
+    if (A->s->cfg.rlx_scheme == JLB_TRT)
+        wo = A->magic > 0.0 ? 1.0 / (A->magic / (tau - 0.5) + 0.5) : 8.0 * (2.0 - we) / (8.0 - we);
+}
+
+} // namespace
+
+extern "C" {
+
+void jlb_adj_destroy(jlb_adjoint *A) {
+    if (!A) return;
+    if (A->s) cudaStreamSynchronize(A->s->st);
+    for (void *p : A->ckpt) if (p) cudaFree(p);
+    for (void *p : A->tee) if (p) cudaFree(p);
+    void *bufs[] = {A->f0, A->lam, A->d_target, A->d_grad, A->d_guin};
+    for (void *p : bufs) if (p) cudaFree(p);
+    if (A->s) jlb_destroy(A->s);
+    delete A;
+}
+
+int jlb_adj_create(const jlb_config *cfg, const uint8_t *phase, int32_t loss_plane, int32_t checkpoint_every,
+                   jlb_adjoint **out) {
+    jlb_adjoint *A = nullptr;
+    if (!cfg || !phase || !out) return afail(nullptr, JLB_ERR_INVALID_ARG, "NULL argument");
+    *out = nullptr;
+    if (cfg->precision == JLB_FP16) return afail(nullptr, JLB_ERR_UNSUPPORTED, "adjoint supports FP64 and FP32");
+    if (cfg->rlx_scheme == JLB_REGULARIZATION)
+        return afail(nullptr, JLB_ERR_UNSUPPORTED, "adjoint supports BGK and TRT");
+    if (checkpoint_every < 1) return afail(nullptr, JLB_ERR_INVALID_ARG, "checkpoint interval must be >= 1");
+    for (int f = 1; f < 6; ++f)
+        if (cfg->bc[f] == JLB_FIXED_VEL)
+            return afail(nullptr, JLB_ERR_UNSUPPORTED, "adjoint: FIXED_VEL is supported on face 1X only");
+    if (cfg->bc[0] == JLB_FIXED_VEL && cfg->bc[1] != JLB_PERIODIC && cfg->lat_size[0] == 1)
+        return afail(nullptr, JLB_ERR_UNSUPPORTED, "adjoint: a one-site-thick domain with two Zou-He faces");
+    if (loss_plane < 0 || loss_plane >= cfg->lat_size[0]) return afail(nullptr, JLB_ERR_INVALID_ARG, "loss plane out of range");
+    A = new jlb_adjoint();
+    A->K = checkpoint_every;
+    A->plane = loss_plane;
+    A->magic = cfg->trt_magic;
+    int r = jlb_create(cfg, &A->s);
+    if (r) { std::string m = g_create_error; delete A; return afail(nullptr, r, m); }
+    jlb_solver *s = A->s;
+    // rest state: den = 1, vel = 0 everywhere, so the initial populations do
+    // not depend on the parameters
+    std::vector<uint8_t> ph((size_t)s->NCNT, 0);
+    std::vector<double> den((size_t)s->NCNT, 1.0), vel(3 * (size_t)s->NCNT, 0.0);
+    for (int i = 0; i < s->nx; ++i)
+        for (int j = 0; j < s->ny; ++j)
+            for (int k = 0; k < s->nz; ++k)
+                ph[fidx(s, i + 1, j + 1, k + 1)] = phase[((size_t)i * s->ny + j) * s->nz + k];
+    uint64_t nf = 0;
+    if ((r = jlb_finalize_init(s, ph.data(), den.data(), vel.data(), &nf))) {
+        std::string m = s->err;
+        jlb_adj_destroy(A);
+        return afail(nullptr, r, m);
+    }
+    A->fbytes = (size_t)19 * s->Np * s->ssz;
+    auto bail = [&](const char *m) { jlb_adj_destroy(A); return afail(nullptr, JLB_ERR_NOMEM, m); };
+    if (cudaMalloc(&A->f0, A->fbytes) != cudaSuccess || cudaMalloc(&A->lam, A->fbytes) != cudaSuccess ||
+        cudaMalloc(&A->d_target, 3 * sizeof(double) * (size_t)s->ny * s->nz) != cudaSuccess ||
+        cudaMalloc(&A->d_grad, 8 * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&A->d_guin, sizeof(double) * (size_t)s->ny * s->nz) != cudaSuccess) {
+        cudaGetLastError();
+        return bail("adjoint state allocation failed");
+    }
+    cudaMemcpy(A->f0, s->f, A->fbytes, cudaMemcpyDeviceToDevice);
+    *out = A;
+    return JLB_OK;
+}
+
+int jlb_adj_forward(jlb_adjoint *A, double tau, const double g[3], const double *uin, double rho_out, uint32_t steps,
+                    const double *target, double *loss, double *u_plane) {
+    if (!A || !g || !uin || steps < 1) return afail(A, JLB_ERR_INVALID_ARG, "bad argument");
+    if (!(tau > 0.5)) return afail(A, JLB_ERR_INVALID_ARG, "tau must exceed 1/2");
+    jlb_solver *s = A->s;
+    double we, wo;
+    adj_rates(A, tau, we, wo);
+    s->we = we;
+    s->wo = wo;
+    for (int d = 0; d < 3; ++d) s->g[d] = g[d];
+    ++s->args_version;
+    // Zou-He data: inlet 1X velocity (uin[j*nz+k], 0, 0), outlet density rho_out
+    const int M = s->M;
+    const size_t nb = 4 * (size_t)std::max(s->bc_slots, 1) * M;
+    std::vector<double> bc(nb, 0.0);
+    for (int t = 0; t < M; ++t) {
+        const int64_t n = s->sp_node[t];
+        const int j = (int)((n / s->nz) % s->ny), k = (int)(n % s->nz);
+        const uint32_t faces = (s->sp_info[t] >> SP_FACE_SHIFT) & 0x3Fu;
+        int slot = 0;
+        for (int face = 0; face < 6; ++face) {
+            if (!(faces & (1u << face))) continue;
+            const bool vel_face = s->cfg.bc[face] == JLB_FIXED_VEL;
+            bc[(size_t)(4 * slot) * M + t] = vel_face ? 1.0 : rho_out;
+            bc[(size_t)(4 * slot + 1) * M + t] = vel_face ? uin[(size_t)j * s->nz + k] : 0.0;
+            slot = 1;
+        }
+    }
+    if (M > 0) {
+        ACK(cudaMemcpyAsync(s->d_sp_bc, bc.data(), nb * sizeof(double), cudaMemcpyHostToDevice, s->st));
+        ACK(cudaMemsetAsync(s->d_sp_den, 0, (size_t)M * s->csz, s->st));
+    }
+    // forward with checkpoints
+    ACK(cudaMemcpyAsync(s->f, A->f0, A->fbytes, cudaMemcpyDeviceToDevice, s->st));
+    s->parity = 0;
+    s->tee = nullptr;
+    const int nseg = (int)((steps + A->K - 1) / A->K);
+    while ((int)A->ckpt.size() < nseg) {
+        void *p = nullptr;
+        ACK(cudaMalloc(&p, A->fbytes));
+        A->ckpt.push_back(p);
+    }
+    for (int seg = 0; seg < nseg; ++seg) {
+        ACK(cudaMemcpyAsync(A->ckpt[seg], s->f, A->fbytes, cudaMemcpyDeviceToDevice, s->st));
+        const uint32_t t0 = (uint32_t)seg * A->K, t1 = std::min<uint32_t>(steps, t0 + A->K);
+        int r = run_steps(s, t1 - t0, t1 == steps);
+        if (r) return afail(A, r, s->err);
+    }
+    // stored velocity on the loss plane, and the loss
+    const size_t plane_n = (size_t)s->ny * s->nz;
+    const int64_t p0 = (int64_t)A->plane * s->ny * s->nz;
+    std::vector<double> up(3 * plane_n);
+    std::vector<uint32_t> pm(plane_n);
+    ACK(cudaMemcpyAsync(pm.data(), s->nmask + p0, plane_n * 4, cudaMemcpyDeviceToHost, s->st));
+    for (int c = 0; c < 3; ++c) {
+        if (s->prec == PREC_FP64) {
+            ACK(cudaMemcpyAsync(up.data() + c * plane_n, (double *)s->mom[1 + c] + p0, plane_n * 8,
+                                cudaMemcpyDeviceToHost, s->st));
+        } else {
+            std::vector<float> tmp(plane_n);
+            ACK(cudaMemcpyAsync(tmp.data(), (float *)s->mom[1 + c] + p0, plane_n * 4, cudaMemcpyDeviceToHost, s->st));
+            ACK(cudaStreamSynchronize(s->st));
+            for (size_t m = 0; m < plane_n; ++m) up[c * plane_n + m] = tmp[m];
+        }
+    }
+    ACK(cudaStreamSynchronize(s->st));
+    double L = 0.0;
+    for (size_t m = 0; m < plane_n; ++m) {
+        if (pm[m] & MASK_SOLID) continue;
+        for (int c = 0; c < 3; ++c) {
+            const double u = up[c * plane_n + m];
+            if (u_plane) u_plane[3 * m + c] = u;
+            if (target) { const double d = u - target[3 * m + c]; L += d * d; }
+        }
+    }
+    std::vector<double> tg(3 * plane_n, 0.0);
+    if (target)
+        for (size_t m = 0; m < plane_n; ++m)
+            if (!(pm[m] & MASK_SOLID)) for (int c = 0; c < 3; ++c) tg[3 * m + c] = target[3 * m + c];
+    ACK(cudaMemcpy(A->d_target, tg.data(), tg.size() * sizeof(double), cudaMemcpyHostToDevice));
+    if (loss) *loss = L;
+    A->steps = steps;
+    A->tau = tau;
+    A->have_forward = true;
+    return JLB_OK;
+}
+
+int jlb_adj_backward(jlb_adjoint *A, double *dtau, double dg[3], double *duin) {
+    if (!A) return afail(A, JLB_ERR_INVALID_ARG, "NULL adjoint");
+    if (!A->have_forward) return afail(A, JLB_ERR_STATE, "run jlb_adj_forward first");
+    jlb_solver *s = A->s;
+    const uint32_t steps = A->steps;
+    const int nseg = (int)((steps + A->K - 1) / A->K);
+    while ((int)A->tee.size() < A->K) {
+        void *p = nullptr;
+        ACK(cudaMalloc(&p, A->fbytes));
+        A->tee.push_back(p);
+    }
+    ACK(cudaMemsetAsync(A->lam, 0, A->fbytes, s->st));
+    ACK(cudaMemsetAsync(A->d_grad, 0, 8 * sizeof(double), s->st));
+    ACK(cudaMemsetAsync(A->d_guin, 0, sizeof(double) * (size_t)s->ny * s->nz, s->st));
+    const int blocks = make_args(s, 0).nb_dense + (s->M + 127) / 128;
+    for (int seg = nseg - 1; seg >= 0; --seg) {
+        const uint32_t t0 = (uint32_t)seg * A->K, t1 = std::min<uint32_t>(steps, t0 + A->K);
+        // recompute the segment, keeping every step's collision inputs
+        ACK(cudaMemcpyAsync(s->f, A->ckpt[seg], A->fbytes, cudaMemcpyDeviceToDevice, s->st));
+        s->parity = (int)(t0 & 1u);
+        for (uint32_t t = t0; t < t1; ++t) {
+            s->tee = A->tee[t - t0];
+            int r = launch_one(s, make_args(s, 0), s->parity == 0);
+            s->tee = nullptr;
+            if (r) return afail(A, r, s->err);
+            s->parity ^= 1;
+        }
+        // reverse sweep over the segment
+        for (int64_t t = (int64_t)t1 - 1; t >= (int64_t)t0; --t) {
+            AdjArgs a{};
+            a.s = make_args(s, 0);
+            a.s.tee = nullptr;
+            a.gin = A->tee[t - t0];
+            a.lam = A->lam;
+            a.seed = (uint32_t)t == steps - 1;
+            a.plane = A->plane;
+            a.target = A->d_target;
+            a.grad = A->d_grad;
+            a.grad_uin = A->d_guin;
+            const int r = launch_adjoint_step(a, s->prec, s->cfg.rlx_scheme, (t & 1) == 0, blocks, s->st);
+            if (r) return afail(A, JLB_ERR_CUDA, std::string("adjoint step: ") + cudaGetErrorString((cudaError_t)r));
+            ++s->launches;
+        }
+    }
+    double gr[8];
+    ACK(cudaMemcpyAsync(gr, A->d_grad, 8 * sizeof(double), cudaMemcpyDeviceToHost, s->st));
+    if (duin) ACK(cudaMemcpyAsync(duin, A->d_guin, sizeof(double) * (size_t)s->ny * s->nz, cudaMemcpyDeviceToHost, s->st));
+    ACK(cudaStreamSynchronize(s->st));
+    // chain rule to tau: we = 1/tau, wo(tau) from the magic parameter
+    double we, wo;
+    adj_rates(A, A->tau, we, wo);
+    double dwo_dtau = 0.0;
+    if (s->cfg.rlx_scheme == JLB_TRT) {
+        const double magic = A->magic > 0.0 ? A->magic : 3.0 / 16.0;
+        dwo_dtau = wo * wo * magic / ((A->tau - 0.5) * (A->tau - 0.5));
+    }
+    if (dtau) {
+        if (s->cfg.rlx_scheme == JLB_TRT) *dtau = gr[0] * (-we * we) + gr[1] * dwo_dtau;
+        else *dtau = (gr[0] + gr[1]) * (-we * we);
+    }
+    if (dg) for (int d = 0; d < 3; ++d) dg[d] = gr[2 + d];
+    return JLB_OK;
+}
+
+const char *jlb_adj_last_error(const jlb_adjoint *A) { return A ? A->err.c_str() : g_create_error.c_str(); }
 
 } // extern "C"

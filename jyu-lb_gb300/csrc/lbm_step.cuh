@@ -154,6 +154,10 @@ __device__ __forceinline__ void dense_node(const StepArgs &a, int b) {
         }
         fv[q] = ST::template ld<q>(f + e);
     });
+    if (a.tee) {
+        S *tee = (S *)a.tee;
+        Unroll<0, Q>::run([&]<int q>() { ST::template st<q>(tee + ((IT)q * Np + n), fv[q]); });
+    }
 
     C ax, ay, az;
     if (ACCF) {
@@ -233,6 +237,10 @@ __device__ __forceinline__ void special_node(const StepArgs &a, int b) {
                 slot = 1;
             }
         }
+    }
+    if (a.tee) {
+        S *tee = (S *)a.tee;
+        Unroll<0, Q>::run([&]<int q>() { ST::template st<q>(tee + ((int64_t)q * Np + n), fv[q]); });
     }
 
     C ax, ay, az;

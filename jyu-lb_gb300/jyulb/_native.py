@@ -28,6 +28,7 @@ EXPORTED_SYMBOLS = (
     "jlb_transfer_bytes", "jlb_host_timers",
     "jlb_last_error", "jlb_batch_create", "jlb_batch_destroy", "jlb_batch_step", "jlb_batch_moments",
     "jlb_batch_populations", "jlb_batch_info", "jlb_batch_domain_fluid", "jlb_batch_last_error",
+    "jlb_adj_create", "jlb_adj_destroy", "jlb_adj_forward", "jlb_adj_backward", "jlb_adj_last_error",
     "jlb_build_info",
 )
 
@@ -105,6 +106,12 @@ def load() -> ctypes.CDLL:
         "jlb_batch_info": (ctypes.c_int, [vp, ctypes.POINTER(ctypes.c_int64)]),
         "jlb_batch_domain_fluid": (ctypes.c_int32, [vp, ctypes.c_int32]),
         "jlb_batch_last_error": (ctypes.c_char_p, [vp]),
+        "jlb_adj_create": (ctypes.c_int, [cfgp, u8p, ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(vp)]),
+        "jlb_adj_destroy": (None, [vp]),
+        "jlb_adj_forward": (ctypes.c_int, [vp, ctypes.c_double, dp, dp, ctypes.c_double, ctypes.c_uint32, dp, dp,
+                                           dp]),
+        "jlb_adj_backward": (ctypes.c_int, [vp, dp, dp, dp]),
+        "jlb_adj_last_error": (ctypes.c_char_p, [vp]),
         "jlb_build_info": (ctypes.c_char_p, []),
     }
     for name, (res, args) in sig.items():

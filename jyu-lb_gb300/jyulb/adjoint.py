@@ -1,0 +1,107 @@
+"""Gradients of a velocity-field loss through the D3Q19 time step.
+
+``ChannelProblem`` is a domain (BGK or TRT, FP32-shifted or FP64) started from
+rest, with a FIXED_VEL inlet on face 1X whose u_x is a parameter per inlet
+site.  The forward run advances ``steps`` steps and scores the stored velocity
+on the plane x = ``loss_plane``:  L = sum over fluid sites of |u - target|^2.
+The backward run is the hand-written discrete adjoint of the fused step
+(reverse AA sweep with the transposed collision, Zou-He and bounce-back
+maps), with checkpoints every ``checkpoint_every`` steps and recomputation
+in between.  ``loss_fn`` wraps both in a ``torch.autograd.Function`` whose
+inputs are the relaxation time ``tau``, the body force ``g`` (3,) and the
+inlet velocities ``uin`` (ny, nz).
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _native
+from .defs import FIXED_DEN, FIXED_VEL, FP32, TRT, WALL, PERIODIC
+
+
+class ChannelProblem:
+    def __init__(self, phase, bc=None, rlx_scheme=TRT, precision=FP32, trt_magic=None, loss_plane=None,
+                 checkpoint_every=50, stream=None):
+        self._lib = _native.load()
+        self.phase = np.ascontiguousarray(phase, dtype=np.uint8)
+        nx, ny, nz = self.phase.shape
+        self.shape = (nx, ny, nz)
+        self.bc = [FIXED_VEL, FIXED_DEN, WALL, WALL, PERIODIC, PERIODIC] if bc is None else [int(b) for b in bc]
+        self.loss_plane = int(nx * 3 // 4 if loss_plane is None else loss_plane)
+        cfg = _native.jlb_config()
+        cfg.lat_size[:] = [nx, ny, nz]
+        cfg.rlx_scheme = int(rlx_scheme)
+        cfg.kvisc = 0.1  # replaced by tau at every forward run
+        cfg.g[:] = [0.0, 0.0, 0.0]
+        cfg.bc[:] = self.bc
+        cfg.precision = int(precision)
+        cfg.trt_magic = 0.0 if trt_magic is None else float(trt_magic)
+        cfg.stream = None if stream is None else int(stream)
+        h = ctypes.c_void_p()
+        rc = self._lib.jlb_adj_create(ctypes.byref(cfg), _native.u8ptr(self.phase), self.loss_plane,
+                                      int(checkpoint_every), ctypes.byref(h))
+        if rc != _native.JLB_OK:
+            raise (ValueError if rc == _native.JLB_ERR_INVALID_ARG else RuntimeError)(
+                self._lib.jlb_adj_last_error(None).decode())
+        self._h = h
+        self.steps = 0
+
+    def __del__(self):
+        h = getattr(self, '_h', None)
+        if h is not None:
+            self._lib.jlb_adj_destroy(h)
+            self._h = None
+
+    def _check(self, rc):
+        if rc != _native.JLB_OK:
+            raise RuntimeError(self._lib.jlb_adj_last_error(self._h).decode())
+
+    def forward(self, tau, g, uin, steps, target=None, rho_out=1.0):
+        """Runs the forward model; returns (loss, u on the loss plane)."""
+        _, ny, nz = self.shape
+        g = np.ascontiguousarray(g, dtype=np.float64).reshape(3)
+        uin = np.ascontiguousarray(uin, dtype=np.float64).reshape(ny, nz)
+        tgt = None if target is None else np.ascontiguousarray(target, dtype=np.float64).reshape(ny, nz, 3)
+        loss = ctypes.c_double()
+        up = np.zeros((ny, nz, 3))
+        self._check(self._lib.jlb_adj_forward(self._h, float(tau), _native.dptr(g), _native.dptr(uin),
+                                              float(rho_out), int(steps),
+                                              _native.dptr(tgt) if tgt is not None else None,
+                                              ctypes.byref(loss), _native.dptr(up)))
+        self.steps = int(steps)
+        return float(loss.value), up
+
+    def backward(self):
+        """Gradients of the last forward run's loss: (dtau, dg (3,), duin (ny,nz))."""
+        _, ny, nz = self.shape
+        dtau = ctypes.c_double()
+        dg = np.zeros(3)
+        duin = np.zeros((ny, nz))
+        self._check(self._lib.jlb_adj_backward(self._h, ctypes.byref(dtau), _native.dptr(dg), _native.dptr(duin)))
+        return float(dtau.value), dg, duin
+
+
+def loss_fn(problem, tau, g, uin, target, steps, rho_out=1.0):
+    """L(tau, g, uin) as a differentiable torch scalar (torch tensors in,
+    gradients from the adjoint)."""
+    import torch
+
+    class _AdjointLoss(torch.autograd.Function):
+        @staticmethod
+        def forward(ctx, tau_t, g_t, uin_t):
+            loss, _ = problem.forward(float(tau_t.detach().cpu()), g_t.detach().cpu().double().numpy(),
+                                      uin_t.detach().cpu().double().numpy(), steps, target, rho_out)
+            ctx.dev, ctx.dtype = tau_t.device, tau_t.dtype
+            return torch.tensor(loss, dtype=torch.float64, device=tau_t.device)
+
+        @staticmethod
+        def backward(ctx, grad_out):
+            dtau, dg, duin = problem.backward()
+            s = float(grad_out)
+            return (torch.tensor(s * dtau, dtype=torch.float64, device=ctx.dev),
+                    torch.tensor(s * dg, dtype=torch.float64, device=ctx.dev),
+                    torch.tensor(s * duin, dtype=torch.float64, device=ctx.dev))
+
+    return _AdjointLoss.apply(tau, g, uin)

@@ -1,0 +1,130 @@
+"""Pure-torch FP64 D3Q19 step used as an autograd checker for the adjoint.
+
+TEST INFRASTRUCTURE ONLY.  Pull streaming with halfway bounce-back and
+periodic wrap, Zou-He velocity inlet on face 1X (per-site u_x) and density
+outlet on face X1, TRT (or BGK) collision with forcing -- the physics of
+jyulb/isothermal.pyx:1112-1326 and jyulb/D3Q19.pyx:655-853 -- written with
+differentiable tensor operations so that torch autograd yields reference
+gradients of the plane-velocity loss.
+"""
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+CI = [-1, -1, -1, -1, -1, 0, 0, 0, 0, 0, 0, 0, 0, 0, 1, 1, 1, 1, 1]
+CJ = [-1, 0, 0, 0, 1, -1, -1, -1, 0, 0, 0, 1, 1, 1, -1, 0, 0, 0, 1]
+CK = [0, -1, 0, 1, 0, -1, 0, 1, -1, 0, 1, -1, 0, 1, 0, -1, 0, 1, 0]
+NNZ = [abs(a) + abs(b) + abs(c) for a, b, c in zip(CI, CJ, CK)]
+W = [1 / 3 if n == 0 else (1 / 18 if n == 1 else 1 / 36) for n in NNZ]
+
+
+def solid_source(phase, periodic):
+    """(19, nx, ny, nz) bool: the upstream site x - c_q is solid (sites
+    outside a non-periodic face count as solid)."""
+    nx, ny, nz = phase.shape
+    I, J, K = np.meshgrid(np.arange(nx), np.arange(ny), np.arange(nz), indexing='ij')
+    out = np.zeros((19, nx, ny, nz), bool)
+    for q in range(19):
+        bad = np.zeros(phase.shape, bool)
+        src = []
+        for ax, (c, n, X) in enumerate(zip((CI[q], CJ[q], CK[q]), (nx, ny, nz), (I, J, K))):
+            s = X - c
+            if periodic[ax]:
+                s = s % n
+            else:
+                bad |= (s < 0) | (s >= n)
+                s = np.clip(s, 0, n - 1)
+            src.append(s)
+        out[q] = bad | (phase[src[0], src[1], src[2]] == 0)
+    return torch.from_numpy(out)
+
+
+def stream(f, solid):
+    g = []
+    for q in range(19):
+        moved = torch.roll(f[q], shifts=(CI[q], CJ[q], CK[q]), dims=(0, 1, 2))
+        g.append(torch.where(solid[q], f[18 - q], moved))
+    return torch.stack(g)
+
+
+def zh_plane(gp, face, jx, jy, jz):
+    """Zou-He unknowns on a face plane (jyulb/bcs.pyx:487-562), gp: list of 19 (ny,nz)."""
+    g = list(gp)
+    if face == 0:
+        t = g[11] + g[12] + g[13] - g[5] - g[6] - g[7]
+        u = g[7] + g[10] + g[13] - g[5] - g[8] - g[11]
+        g[14] = g[4] + jx / 6 + 0.5 * t - 0.5 * jy
+        g[18] = g[0] + jx / 6 - 0.5 * t + 0.5 * jy
+        g[15] = g[3] + jx / 6 + 0.5 * u - 0.5 * jz
+        g[17] = g[1] + jx / 6 - 0.5 * u + 0.5 * jz
+        g[16] = g[2] + jx / 3
+    else:
+        t = g[11] + g[12] + g[13] - g[5] - g[6] - g[7]
+        u = g[7] + g[10] + g[13] - g[5] - g[8] - g[11]
+        g[0] = g[18] - jx / 6 + 0.5 * t - 0.5 * jy
+        g[4] = g[14] - jx / 6 - 0.5 * t + 0.5 * jy
+        g[1] = g[17] - jx / 6 + 0.5 * u - 0.5 * jz
+        g[3] = g[15] - jx / 6 - 0.5 * u + 0.5 * jz
+        g[2] = g[16] - jx / 3
+    return g
+
+
+def apply_zou_he(g, uin, rho_out):
+    zero = [q for q in range(19) if CI[q] == 0]
+    # inlet 1X: fixed velocity (uin, 0, 0)
+    p = [g[q][0] for q in range(19)]
+    S = sum(p[q] for q in zero) + 2 * sum(p[q] for q in range(19) if CI[q] == -1)
+    rho_bc = S / (1.0 - uin)
+    p = zh_plane(p, 0, rho_bc * uin, torch.zeros_like(uin), torch.zeros_like(uin))
+    # outlet X1: fixed density, zero tangential velocity
+    o = [g[q][-1] for q in range(19)]
+    S = sum(o[q] for q in zero) + 2 * sum(o[q] for q in range(19) if CI[q] == 1)
+    z = torch.zeros_like(S)
+    o = zh_plane(o, 1, S - rho_out, z, z)
+    out = []
+    for q in range(19):
+        out.append(torch.cat([p[q][None], g[q][1:-1], o[q][None]], dim=0))
+    return torch.stack(out)
+
+
+def collide(g, a, we, wo):
+    C = torch.tensor([CI, CJ, CK], dtype=g.dtype, device=g.device)  # (3,19)
+    w = torch.tensor(W, dtype=g.dtype, device=g.device)
+    rho = g.sum(0)
+    j = torch.einsum('aq,qxyz->axyz', C, g)
+    u = j / rho + 0.5 * a[:, None, None, None]
+    s = rho * u
+    c1, c2 = 1 - 0.5 * wo, 1 - 0.5 * we
+    c3, c4 = 1 - 0.5 * (we + wo), 0.5 * (we - wo)
+    H0 = we * rho
+    H1 = wo * s + c1 * rho * a[:, None, None, None]
+    H2 = we * torch.einsum('axyz,bxyz->abxyz', s, s) / rho + c2 * (
+        torch.einsum('a,bxyz->abxyz', a, s) + torch.einsum('b,axyz->abxyz', a, s))
+    cc = torch.einsum('aq,bq->abq', C, C) - torch.eye(3, dtype=g.dtype, device=g.device)[:, :, None] / 3
+    P = w[:, None, None, None] * (H0[None] + 3 * torch.einsum('aq,axyz->qxyz', C, H1)
+                                  + 4.5 * torch.einsum('abq,abxyz->qxyz', cc, H2))
+    opp = torch.arange(18, -1, -1)
+    relax = c3 * g - c4 * g[opp]
+    relax = torch.cat([relax[:9], ((1 - we) * g[9])[None], relax[10:]])
+    return relax + P, rho, u
+
+
+def run(phase, tau, g, uin, steps, magic=None, scheme='TRT', rho_out=1.0, periodic=(False, False, True)):
+    """Returns the stored velocity of the last step, (3, nx, ny, nz)."""
+    solid = solid_source(phase, periodic)
+    fluid = torch.from_numpy(phase != 0)
+    we = 1.0 / tau
+    if scheme == 'TRT':
+        wo = 1.0 / (magic / (tau - 0.5) + 0.5) if magic else 8.0 * (2.0 - we) / (8.0 - we)
+    else:
+        wo = we
+    w = torch.tensor(W, dtype=torch.float64)
+    f = w[:, None, None, None].expand(19, *phase.shape).clone()
+    u = None
+    for _ in range(steps):
+        gs = stream(f, solid)
+        gs = apply_zou_he(gs, uin, rho_out)
+        f, rho, u = collide(gs, g, we, wo)
+        f = torch.where(fluid[None], f, w[:, None, None, None].expand_as(f))
+    return u
