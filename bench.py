@@ -312,12 +312,147 @@ def run_ensemble(args):
                                "gx~U[1e-7,1e-5], half with moving top wall u~U[0.01,0.05]; BGK",
                    "domains": len(doms), "packed_sites": info["sites"], "fluid_sites": nf,
                    "setup_s": round(setup_s, 1), "autotuned_block": info["block"],
-                   "autotune_ns_per_step": info["tune_ns_per_step"]},
+                   "autotune_us_per_step": info["tune_us_per_step"]},
         "roofline": {"bound": "hbm", "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(ach / peak, 4), "peak_kind": peak_kind, "bytes_per_site": BYTES_FP32},
         "error": {"domains_checked": len(errs), "vel_rel_l2_vs_fp64_max": max(errs) if errs else None,
                   "vel_rel_l2_vs_fp64_median": statistics.median(errs) if errs else None, "steps": total},
         "gpu_launches": launches, "clocks": clk.summary(),
+    }
+    print(json.dumps(line))
+    return 0
+
+
+ADJ_SHAPE = (256, 64, 64)
+ADJ_PLANE = 200
+BYTES_ADJ_FP32 = 228  # reverse sweep: adjoint populations read + written, state before the step read
+BYTES_RECOMP_FP32 = 152  # recompute: one out-of-place forward step (K-1 of every K steps)
+
+
+def adjoint_case(precision, stream=None, K=50):
+    """The inverse-problem channel: 256x64x64, a cylinder of radius 8 along z
+    at a seeded position, Zou-He velocity inlet on x=0 with one u_x per inlet
+    site, density outlet rho=1 on the last x layer, walls on the y and z faces;
+    TRT with magic parameter 1/4; loss on the plane x=200."""
+    from jyulb.adjoint import ChannelProblem
+    from jyulb.defs import FIXED_DEN, FIXED_VEL, TRT, WALL
+
+    nx, ny, nz = ADJ_SHAPE
+    rng = np.random.default_rng(7)
+    cx, cy = int(rng.integers(56, 73)), ny // 2 + int(rng.integers(-3, 4))
+    X, Y = np.meshgrid(np.arange(nx), np.arange(ny), indexing="ij")
+    phase = np.ones(ADJ_SHAPE, np.uint8)
+    phase[(X - cx) ** 2 + (Y - cy) ** 2 <= 64] = 0
+    return ChannelProblem(phase, bc=[FIXED_VEL, FIXED_DEN, WALL, WALL, WALL, WALL], rlx_scheme=TRT,
+                          precision=precision, trt_magic=0.25, loss_plane=ADJ_PLANE, checkpoint_every=K,
+                          stream=stream), phase
+
+
+def adjoint_params():
+    """Hidden parameters (they make the target) and the starting guess."""
+    _, ny, nz = ADJ_SHAPE
+    rng = np.random.default_rng(11)
+    yy = (np.arange(ny) + 0.5) / ny
+    zz = (np.arange(nz) + 0.5) / nz
+    prof = 16.0 * np.outer(yy * (1 - yy), zz * (1 - zz))
+    hidden = (0.6 + 0.05 * float(rng.random()), np.array([2e-6 * (1 + 0.2 * float(rng.random())), 0.0, 0.0]),
+              0.04 * prof * (1 + 0.1 * rng.standard_normal((ny, nz))))
+    guess = (0.58, np.array([1e-6, 0.0, 0.0]), 0.035 * prof)
+    return hidden, guess
+
+
+def run_adjoint(args):
+    """Adjoint workload: forward and backward device times of the FP32
+    problem, and its gradients against central differences of the FP64
+    forward model."""
+    import torch
+    from jyulb.defs import FP32, FP64
+
+    torch.cuda.set_device(0)
+    steps = args.adj_steps
+    st = torch.cuda.Stream()
+    p32, phase = adjoint_case(FP32, st.cuda_stream)
+    nf = int((phase != 0).sum())
+    (tau_h, g_h, uin_h), (tau0, g0, uin0) = adjoint_params()
+    _, target = p32.forward(tau_h, g_h, uin_h, steps)
+    for _ in range(max(1, args.warmup // 5)):
+        p32.forward(tau0, g0, uin0, steps, target)
+        p32.backward()
+    recs = []
+    walls = []
+    with ClockSampler(0) as clk:
+        for _ in range(args.adj_reps):
+            t0 = time.perf_counter()
+            L, _ = p32.forward(tau0, g0, uin0, steps, target)
+            dtau, dg, duin = p32.backward()
+            walls.append(time.perf_counter() - t0)
+            recs.append(p32.timers())
+    med = {k: statistics.median(r[k] for r in recs) for k in recs[0]}
+    ratio = med["backward"] / med["forward"]
+    # central differences of the FP64 forward model
+    p64, _ = adjoint_case(FP64)
+    L64, _ = p64.forward(tau0, g0, uin0, steps, target)
+    a64 = p64.backward()
+
+    def loss64(tau, g, uin):
+        return p64.forward(tau, g, uin, steps, target)[0]
+
+    rng = np.random.default_rng(3)
+    v = rng.choice([-1.0, 1.0], size=uin0.shape) * (phase[0] != 0)
+    big = np.unravel_index(np.argsort(np.abs(duin).ravel())[-2:], duin.shape)
+    checks = []
+
+    def fd(name, h, plus, minus, adj32, adj64):
+        d = (loss64(*plus) - loss64(*minus)) / (2 * h)
+        checks.append({"param": name, "fd_fp64": d, "adjoint_fp32": adj32, "adjoint_fp64": adj64,
+                       "rel_err_fp32": abs(adj32 - d) / abs(d), "rel_err_fp64": abs(adj64 - d) / abs(d)})
+
+    h = 1e-4
+    fd("tau", h, (tau0 + h, g0, uin0), (tau0 - h, g0, uin0), dtau, a64[0])
+    h = 1e-9
+    e = np.array([h, 0.0, 0.0])
+    fd("gx", h, (tau0, g0 + e, uin0), (tau0, g0 - e, uin0), dg[0], a64[1][0])
+    h = 1e-6
+    fd("uin.v (random +-1 direction over the inlet)", h, (tau0, g0, uin0 + h * v), (tau0, g0, uin0 - h * v),
+       float((duin * v).sum()), float((a64[2] * v).sum()))
+    for j, k in zip(*big):
+        du = np.zeros_like(uin0)
+        du[j, k] = h
+        fd(f"uin[{j},{k}]", h, (tau0, g0, uin0 + du), (tau0, g0, uin0 - du), float(duin[j, k]), float(a64[2][j, k]))
+    peak, peak_kind = measured_peak()
+    rev_ms = med["reverse"] / steps
+    rec_ms = med["recompute"] / (steps - (steps + 49) // 50)
+    bwd_bytes = nf * (BYTES_ADJ_FP32 * steps + BYTES_RECOMP_FP32 * (steps - (steps + 49) // 50))
+    line = {
+        "metric": "adjoint backward / forward device-time ratio, D3Q19 TRT channel 256x64x64, FP32 shifted",
+        "value": round(ratio, 3), "unit": "x", "n_gpus": 1, "steps": steps, "warmup": max(1, args.warmup // 5),
+        "ms_per_step": round(med["forward"] / steps, 5), "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "channel 256x64x64, seeded cylinder r=8 along z, Zou-He u_x inlet per site, "
+                               "outlet rho=1, walls y/z, TRT magic 1/4; loss |u-target|^2 on x=200, target "
+                               "from hidden seeded (tau, gx, uin)",
+                   "fluid_sites": nf, "checkpoint_every": 50, "repetitions": args.adj_reps,
+                   "l2": "80 MB lattice; 3.1 GB of checkpoints and 7.9 GB of recompute states per run exceed the 129 MB L2"},
+        "forward_ms": round(med["forward"], 3), "backward_ms": round(med["backward"], 3),
+        "recompute_ms": round(med["recompute"], 3), "reverse_ms": round(med["reverse"], 3),
+        "reverse_step_vs_forward_step": round(med["reverse"] / med["forward"], 3),
+        "forward_mlups": round(nf * steps / med["forward"] / 1e3, 1),
+        "reverse_sweep_mlups": round(nf * steps / med["reverse"] / 1e3, 1),
+        "roofline": {"bound": "hbm", "kernel": "adjoint reverse sweep", "achieved": round(
+            nf * BYTES_ADJ_FP32 / (rev_ms * 1e-3) / 1e9, 1), "peak": peak, "unit": "GB/s",
+            "frac": round(nf * BYTES_ADJ_FP32 / (rev_ms * 1e-3) / 1e9 / peak, 4), "peak_kind": peak_kind,
+            "bytes_per_site": BYTES_ADJ_FP32, "recompute_gbs": round(nf * BYTES_RECOMP_FP32 / (rec_ms * 1e-3) / 1e9, 1),
+            "recompute_bytes_per_site": BYTES_RECOMP_FP32,
+            "backward_gbs": round(bwd_bytes / (med["backward"] * 1e-3) / 1e9, 1),
+            "note": "recompute (second stream) overlaps the reverse sweep; kernel times are measured while overlapped"},
+        "loss": {"fp32": L, "fp64": L64},
+        "gradient_check": checks,
+        "max_rel_err_fp32_vs_fd": max(c["rel_err_fp32"] for c in checks),
+        "e2e": {"value": round(statistics.median(walls) * 1e3, 2), "unit": "ms per forward+backward through "
+                "jyulb.adjoint (host parameters in, gradients out)",
+                "h2d_bytes_per_step": int(8 * (uin0.size + target.size + 4)),
+                "d2h_bytes_per_step": int(8 * (uin0.size + 4 + target.size))},
+        "clocks": clk.summary(),
     }
     print(json.dumps(line))
     return 0
@@ -365,7 +500,9 @@ def main():
     ap.add_argument("--err-steps", type=int, default=1000)
     ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="cavity", choices=["cavity", "ensemble"])
+    ap.add_argument("--workload", default="cavity", choices=["cavity", "ensemble", "adjoint"])
+    ap.add_argument("--adj-steps", type=int, default=2000)
+    ap.add_argument("--adj-reps", type=int, default=3)
     ap.add_argument("--domains", type=int, default=512)
     ap.add_argument("--check-domains", type=int, default=6)
     args = ap.parse_args()
@@ -375,6 +512,8 @@ def main():
         return run_reference_arm(args)
     if args.workload == "ensemble":
         return run_ensemble(args)
+    if args.workload == "adjoint":
+        return run_adjoint(args)
 
     import torch
 

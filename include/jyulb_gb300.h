@@ -174,7 +174,7 @@ int jlb_batch_moments(jlb_batch *b, int32_t d, double *den, double *vel);
 /* post-collision populations of domain d, (19, nx, ny, nz) FP64 */
 int jlb_batch_populations(jlb_batch *b, int32_t d, double *f);
 /* out: total packed sites, fluid sites, block size, tiles, launches, and the
- * autotuner's per-step times (ns) for blocks of 64, 128, 256 */
+ * autotuner's per-step times (microseconds) for blocks of 64, 128, 256 */
 int jlb_batch_info(const jlb_batch *b, int64_t out[8]);
 int32_t jlb_batch_domain_fluid(const jlb_batch *b, int32_t d);
 const char *jlb_batch_last_error(const jlb_batch *b);
@@ -200,6 +200,10 @@ int jlb_adj_forward(jlb_adjoint *a, double tau, const double g[3], const double 
                     uint32_t steps, const double *target, double *loss, double *u_plane);
 /* gradients of the last forward run's loss; duin: (ny,nz) */
 int jlb_adj_backward(jlb_adjoint *a, double *dtau, double dg[3], double *duin);
+/* device time (ms, CUDA events on the problem's stream) of the last runs:
+ * out[0] forward, out[1] recomputation, out[2] reverse sweep, out[3] the
+ * whole backward run */
+int jlb_adj_timers(const jlb_adjoint *a, double out[4]);
 const char *jlb_adj_last_error(const jlb_adjoint *a);
 
 /* number of steps taken since finalize (Solver.tot_tsteps) */

@@ -8,8 +8,10 @@
 // node: read Lam at the addresses the forward step wrote, apply the
 // transposed collision and Zou-He Jacobians, write Lam at the addresses the
 // forward step read.  Bounce-back links are part of the address maps, so
-// their transpose comes for free.  The collision inputs of the step (after
-// Zou-He) come from the forward recompute (StepArgs::tee).
+// their transpose comes for free.  The collision inputs of the step are
+// gathered again from the state before the step, which the recompute of the
+// segment wrote out of place (StepArgs::fout); boundary sites, whose inputs
+// pass through Zou-He, read a copy the recompute kept (StepArgs::sp_tee).
 //
 // Collision (BGK / TRT with forcing, jyulb/D3Q19.pyx:655-853):
 //   rho = sum g, j = sum c g, s = j + rho a / 2,
@@ -162,25 +164,28 @@ __device__ void zh_adjoint(int fc, int kind, double den, double ux, double uy, d
     }
 }
 
-// transposed collision; g: collision inputs (shifted by w when SHIFTED),
-// lo: adjoint of the outputs, li: adjoint of the inputs (out), pg: local
-// sensitivities to we, wo, ax, ay, az (accumulated), and the stored-velocity
-// seed of the loss (du_loss, or nullptr)
-template <class C, bool SHIFTED, int SCH>
-__device__ void coll_adjoint(const C *g, const C *lo, C ax, C ay, C az, C we, C wo, C *li, double *pg,
-                             const double *du_loss) {
-    if (SCH == SCH_BGK) wo = we;
+// Transposed collision, in two phases so that the inputs g need not stay
+// live: AdjSums accumulates, population by population, the moments of the
+// inputs (rho, j), the moments of the output adjoint lo (L0, L1, L2) and the
+// input-weighted sums the relaxation-rate sensitivities need; adj_finish then
+// forms the adjoint of every input li_q (handed to `put`) and adds the local
+// sensitivities to we, wo, ax, ay, az into pg.  On the loss step a site of the
+// loss plane adds the seed dL/du of its stored velocity u = j/rho + a/2.
+template <class C, bool SHIFTED> struct AdjSums {
     C rho = SHIFTED ? (C)1 : (C)0, jx = 0, jy = 0, jz = 0;
-    C L0 = 0, L1x = 0, L1y = 0, L1z = 0;
-    C Lxx = 0, Lyy = 0, Lzz = 0, Lxy = 0, Lxz = 0, Lyz = 0;
-    Unroll<0, Q>::run([&]<int q>() {
+    C L0 = 0, L1x = 0, L1y = 0, L1z = 0, Lxx = 0, Lyy = 0, Lzz = 0, Lxy = 0, Lxz = 0, Lyz = 0;
+    C sum_pair = 0; // sum_q lo_q (f_q + f_opp(q)), q != rest
+    C dif_pair = 0; // sum_q lo_q (f_opp(q) - f_q)
+    C rest = 0;     // lo_rest f_rest
+    // input g (shifted by w when SHIFTED) and output adjoint l of population q
+    template <int q> __device__ __forceinline__ void add(C g, C l) {
         constexpr C w = (C)WQ<q>();
         constexpr int cx = CX(q), cy = CY(q), cz = CZ(q);
-        rho += g[q];
-        if (cx) jx += (C)cx * g[q];
-        if (cy) jy += (C)cy * g[q];
-        if (cz) jz += (C)cz * g[q];
-        const C wl = w * lo[q];
+        rho += g;
+        if (cx) jx += (C)cx * g;
+        if (cy) jy += (C)cy * g;
+        if (cz) jz += (C)cz * g;
+        const C wl = w * l;
         L0 += wl;
         if (cx) L1x += (C)(3 * cx) * wl;
         if (cy) L1y += (C)(3 * cy) * wl;
@@ -191,34 +196,57 @@ __device__ void coll_adjoint(const C *g, const C *lo, C ax, C ay, C az, C we, C 
         if (cx * cy) Lxy += (C)(4.5 * cx * cy) * wl;
         if (cx * cz) Lxz += (C)(4.5 * cx * cz) * wl;
         if (cy * cz) Lyz += (C)(4.5 * cy * cz) * wl;
-    });
+        if (q == 9) rest = l * (g + (SHIFTED ? w : (C)0));
+    }
+    // the pair (q, OPP(q)), q < 9, once both populations were added
+    template <int q> __device__ __forceinline__ void pair(C gq, C go, C lq, C lo) {
+        constexpr C w2 = SHIFTED ? (C)(2.0 * WQ<q>()) : (C)0;
+        sum_pair += (lq + lo) * (gq + go + w2);
+        dif_pair += (lq - lo) * (go - gq);
+    }
+};
+
+// adds the population pair sums once all 19 inputs and adjoints are at hand
+template <class C, bool SHIFTED>
+__device__ __forceinline__ void adj_accumulate(AdjSums<C, SHIFTED> &S, const C *g, const C *lo) {
+    Unroll<0, Q>::run([&]<int q>() { S.template add<q>(g[q], lo[q]); });
+    Unroll<0, 9>::run([&]<int q>() { S.template pair<q>(g[q], g[OPP(q)], lo[q], lo[OPP(q)]); });
+}
+
+template <class C, bool SHIFTED, int SCH, bool SEED, class PUT>
+__device__ __forceinline__ void adj_finish(const AdjSums<C, SHIFTED> &S, const C *lo, C ax, C ay, C az, C we, C wo,
+                                           C *pg, bool on_plane, const double *tg, double gx, double gy, double gz,
+                                           PUT &&put) {
+    if (SCH == SCH_BGK) wo = we;
+    const C rho = S.rho, jx = S.jx, jy = S.jy, jz = S.jz;
     const C c1 = (C)1 - (C)0.5 * wo, c2 = (C)1 - (C)0.5 * we;
     const C c3 = (C)1 - (C)0.5 * (we + wo), c4 = (C)0.5 * (we - wo);
     const C sx = jx + (C)0.5 * rho * ax, sy = jy + (C)0.5 * rho * ay, sz = jz + (C)0.5 * rho * az;
-    const C Lsx = Lxx * sx + Lxy * sy + Lxz * sz;
-    const C Lsy = Lxy * sx + Lyy * sy + Lyz * sz;
-    const C Lsz = Lxz * sx + Lyz * sy + Lzz * sz;
-    const C Lax = Lxx * ax + Lxy * ay + Lxz * az;
-    const C Lay = Lxy * ax + Lyy * ay + Lyz * az;
-    const C Laz = Lxz * ax + Lyz * ay + Lzz * az;
+    const C Lsx = S.Lxx * sx + S.Lxy * sy + S.Lxz * sz;
+    const C Lsy = S.Lxy * sx + S.Lyy * sy + S.Lyz * sz;
+    const C Lsz = S.Lxz * sx + S.Lyz * sy + S.Lzz * sz;
+    const C Lax = S.Lxx * ax + S.Lxy * ay + S.Lxz * az;
+    const C Lay = S.Lxy * ax + S.Lyy * ay + S.Lyz * az;
+    const C Laz = S.Lxz * ax + S.Lyz * ay + S.Lzz * az;
     const C ir = (C)1 / rho;
-    const C dsx = wo * L1x + (C)2 * we * Lsx * ir + (C)2 * c2 * Lax;
-    const C dsy = wo * L1y + (C)2 * we * Lsy * ir + (C)2 * c2 * Lay;
-    const C dsz = wo * L1z + (C)2 * we * Lsz * ir + (C)2 * c2 * Laz;
+    const C dsx = wo * S.L1x + (C)2 * we * Lsx * ir + (C)2 * c2 * Lax;
+    const C dsy = wo * S.L1y + (C)2 * we * Lsy * ir + (C)2 * c2 * Lay;
+    const C dsz = wo * S.L1z + (C)2 * we * Lsz * ir + (C)2 * c2 * Laz;
     const C sLs = sx * Lsx + sy * Lsy + sz * Lsz;
-    C drho = we * L0 + c1 * (L1x * ax + L1y * ay + L1z * az) - we * sLs * ir * ir +
-             (C)0.5 * (ax * dsx + ay * dsy + az * dsz);
+    const C L1a = S.L1x * ax + S.L1y * ay + S.L1z * az;
+    C drho = we * S.L0 + c1 * L1a - we * sLs * ir * ir + (C)0.5 * (ax * dsx + ay * dsy + az * dsz);
     C djx = dsx, djy = dsy, djz = dsz;
-    // loss seed: stored u = j/rho + a/2
-    double dax_seed = 0, day_seed = 0, daz_seed = 0;
-    if (du_loss) {
+    C dax_seed = 0, day_seed = 0, daz_seed = 0;
+    if (SEED && on_plane) {
+        // L = sum |u - target|^2 over the plane
         const C ux = jx * ir, uy = jy * ir, uz = jz * ir;
-        const C d0 = (C)du_loss[0], d1 = (C)du_loss[1], d2 = (C)du_loss[2];
+        const C d0 = (C)(2.0 * ((double)ux + 0.5 * gx - tg[0]));
+        const C d1 = (C)(2.0 * ((double)uy + 0.5 * gy - tg[1]));
+        const C d2 = (C)(2.0 * ((double)uz + 0.5 * gz - tg[2]));
         djx += d0 * ir; djy += d1 * ir; djz += d2 * ir;
         drho -= (d0 * ux + d1 * uy + d2 * uz) * ir;
-        dax_seed = 0.5 * du_loss[0]; day_seed = 0.5 * du_loss[1]; daz_seed = 0.5 * du_loss[2];
+        dax_seed = (C)0.5 * d0; day_seed = (C)0.5 * d1; daz_seed = (C)0.5 * d2;
     }
-    C sum_pair = 0, dif_pair = 0;
     Unroll<0, Q>::run([&]<int q>() {
         constexpr int cx = CX(q), cy = CY(q), cz = CZ(q);
         C v;
@@ -228,76 +256,135 @@ __device__ void coll_adjoint(const C *g, const C *lo, C ax, C ay, C az, C we, C 
         if (cx) v += (C)cx * djx;
         if (cy) v += (C)cy * djy;
         if (cz) v += (C)cz * djz;
-        li[q] = v;
-        if (q != 9) {
-            constexpr C w = (C)WQ<q>();
-            const C fq = g[q] + (SHIFTED ? w : (C)0), fo = g[OPP(q)] + (SHIFTED ? w : (C)0);
-            sum_pair += lo[q] * (fq + fo);
-            dif_pair += lo[q] * (fo - fq);
-        }
+        put.template operator()<q>(v);
     });
-    const C f9 = g[9] + (SHIFTED ? (C)WQ<9>() : (C)0);
     const C aLs = ax * Lsx + ay * Lsy + az * Lsz;
-    const double dwe = (double)(rho * L0 + sLs * ir - aLs - (C)0.5 * sum_pair - lo[9] * f9);
-    const double dwo = (double)(L1x * sx + L1y * sy + L1z * sz - (C)0.5 * rho * (L1x * ax + L1y * ay + L1z * az) +
-                                (C)0.5 * dif_pair);
-    pg[0] += dwe;
-    pg[1] += dwo;
-    pg[2] += (double)((C)0.5 * rho * dsx + c1 * rho * L1x + (C)2 * c2 * Lsx) + dax_seed;
-    pg[3] += (double)((C)0.5 * rho * dsy + c1 * rho * L1y + (C)2 * c2 * Lsy) + day_seed;
-    pg[4] += (double)((C)0.5 * rho * dsz + c1 * rho * L1z + (C)2 * c2 * Lsz) + daz_seed;
+    pg[0] += rho * S.L0 + sLs * ir - aLs - (C)0.5 * S.sum_pair - S.rest;
+    pg[1] += S.L1x * sx + S.L1y * sy + S.L1z * sz - (C)0.5 * rho * L1a + (C)0.5 * S.dif_pair;
+    pg[2] += (C)0.5 * rho * dsx + c1 * rho * S.L1x + (C)2 * c2 * Lsx + dax_seed;
+    pg[3] += (C)0.5 * rho * dsy + c1 * rho * S.L1y + (C)2 * c2 * Lsy + day_seed;
+    pg[4] += (C)0.5 * rho * dsz + c1 * rho * S.L1z + (C)2 * c2 * Lsz + daz_seed;
 }
 
-template <class ST, int SCH>
-__device__ __forceinline__ void adj_node(const AdjArgs &A, bool pstep, bool special, int64_t n, int t_sp,
-                                         uint32_t m, int i, int j, int k, double *pg) {
+// block sum of the five sensitivities, added by one thread into this block's
+// own double slot (slots are summed on the host after the sweep: no atomics,
+// and the result does not depend on scheduling)
+template <class C> __device__ __forceinline__ void block_sensitivities(C *pg, double *slot) {
+    __shared__ C sm[5][4];
+    const int tid = (int)(threadIdx.y * blockDim.x + threadIdx.x);
+    const int lane = tid & 31, wid = tid >> 5;
+#pragma unroll
+    for (int c = 0; c < 5; ++c) {
+        C v = pg[c];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (lane == 0) sm[c][wid] = v;
+    }
+    __syncthreads();
+    if (tid < 5) slot[tid] += (double)sm[tid][0] + (double)sm[tid][1] + (double)sm[tid][2] + (double)sm[tid][3];
+}
+
+// resident blocks per SM the dense kernel is compiled for: the FP32 sweep
+// fits 5 x 128 threads (<= 96 registers) without spills; the loss-seeding
+// variant, which runs once per sweep, gets 4
+template <class ST, bool SEED> constexpr int adj_min_blocks() { return ST::shifted ? (SEED ? 4 : 5) : 1; }
+
+// Dense sites.  Their collision inputs are gathered from the state before the
+// step (A.snap) exactly as the forward step gathers them; the adjoint of the
+// outputs sits where the forward step wrote (same address maps).
+template <class ST, int SCH, bool PSTEP, bool SEED, class IT>
+__device__ __forceinline__ void adjoint_dense_sites(const AdjArgs &A, int b, typename ST::C *pg) {
     using S = typename ST::S;
     using C = typename ST::C;
     const StepArgs &a = A.s;
-    const int64_t Np = a.Np;
-    S *lam = (S *)A.lam;
-    const S *gin = (const S *)A.gin;
-    C g[Q], lo[Q], li[Q];
-    // dense-node neighbour offsets (periodic wrap), as in the forward step
-    int64_t dI[3] = {0, 0, 0}, dJ[3] = {0, 0, 0}, dK[3] = {0, 0, 0};
-    if (pstep && !special) {
-        const int64_t sI = (int64_t)a.ny * a.nz, sJ = a.nz;
-        dI[0] = (i == 0 ? (int64_t)(a.nx - 1) : -1) * sI; dI[2] = (i + 1 == a.nx ? (int64_t)(1 - a.nx) : 1) * sI;
-        dJ[0] = (j == 0 ? (int64_t)(a.ny - 1) : -1) * sJ; dJ[2] = (j + 1 == a.ny ? (int64_t)(1 - a.ny) : 1) * sJ;
-        dK[0] = k == 0 ? (int64_t)(a.nz - 1) : -1;         dK[2] = k + 1 == a.nz ? (int64_t)(1 - a.nz) : 1;
+    const int kb = b % a.kblocks, rb = b / a.kblocks;
+    const int row = rb * a.by + (int)threadIdx.y;
+    const int k = kb * a.bx + (int)threadIdx.x;
+    if (row < a.nx * a.ny && k < a.nz) {
+        const IT n = (IT)row * a.nz + k;
+        const uint8_t cls = __ldg(a.ncls + n);
+        if (cls < CLS_SPECIAL) {
+            const uint32_t m = (PSTEP && cls == CLS_WALL) ? __ldg(a.nmask + n) : 0u;
+            const IT Np = (IT)a.Np;
+            const int i = row / a.ny, j = row - i * a.ny;
+            IT dI[3], dJ[3], dK[3];
+            if (PSTEP) {
+                const IT sI = (IT)a.ny * a.nz, sJ = (IT)a.nz;
+                dI[0] = (i == 0 ? (IT)(a.nx - 1) : (IT)-1) * sI;
+                dI[1] = 0;
+                dI[2] = (i + 1 == a.nx ? (IT)(1 - a.nx) : (IT)1) * sI;
+                dJ[0] = (j == 0 ? (IT)(a.ny - 1) : (IT)-1) * sJ;
+                dJ[1] = 0;
+                dJ[2] = (j + 1 == a.ny ? (IT)(1 - a.ny) : (IT)1) * sJ;
+                dK[0] = k == 0 ? (IT)(a.nz - 1) : (IT)-1;
+                dK[1] = 0;
+                dK[2] = k + 1 == a.nz ? (IT)(1 - a.nz) : (IT)1;
+            }
+            const S *snap = (const S *)A.snap;
+            S *lam = (S *)A.lam;
+            // forward read (r) and write (w) element of population q
+            auto rd = [&]<int q>() -> IT {
+                if (!PSTEP || q == 9) return (IT)q * Np + n;
+                const IT src = n + dI[1 - CX(q)] + dJ[1 - CY(q)] + dK[1 - CZ(q)];
+                return (m & (1u << q)) ? (IT)q * Np + n : (IT)OPP(q) * Np + src;
+            };
+            auto wr = [&]<int q>() -> IT {
+                if (!PSTEP) return (IT)OPP(q) * Np + n;
+                if (q == 9) return (IT)9 * Np + n;
+                const IT dst = n + dI[1 + CX(q)] + dJ[1 + CY(q)] + dK[1 + CZ(q)];
+                return (m & (1u << OPP(q))) ? (IT)OPP(q) * Np + n : (IT)q * Np + dst;
+            };
+            AdjSums<C, ST::shifted> sums;
+            C lo[Q];
+            {
+                C g[Q];
+                Unroll<0, Q>::run([&]<int q>() {
+                    g[q] = ST::template ld<q>(snap + rd.template operator()<q>());
+                    lo[q] = (C)lam[wr.template operator()<q>()];
+                });
+                adj_accumulate(sums, g, lo);
+            }
+            const double *tg = nullptr;
+            const bool on_plane = SEED && i == A.plane;
+            if (on_plane) tg = A.target + 3 * ((int64_t)j * a.nz + k);
+            adj_finish<C, ST::shifted, SCH, SEED>(sums, lo, (C)a.g[0], (C)a.g[1], (C)a.g[2], (C)a.w_e, (C)a.w_o, pg,
+                                                 on_plane, tg, a.g[0], a.g[1], a.g[2],
+                                                 [&]<int q>(C v) { lam[rd.template operator()<q>()] = (S)v; });
+        }
     }
+}
+
+// Boundary sites: collision inputs from the recompute's copy (A.sp_in),
+// transposed Zou-He after the transposed collision.
+template <class ST, int SCH, bool PSTEP, bool SEED>
+__device__ __forceinline__ void adjoint_boundary_sites(const AdjArgs &A, int b, typename ST::C *pg) {
+    using S = typename ST::S;
+    using C = typename ST::C;
+    const StepArgs &a = A.s;
+    const int tid = (int)(threadIdx.y * blockDim.x + threadIdx.x);
+    const int t = b * (int)(blockDim.x * blockDim.y) + tid;
     const int M = a.M;
-    Unroll<0, Q>::run([&]<int q>() {
-        g[q] = ST::template ld<q>(gin + (int64_t)q * Np + n);
-        // adjoint of output q sits where the forward step wrote f*_q
-        int64_t w;
-        if (!pstep) w = (int64_t)OPP(q) * Np + n;
-        else if (special) w = __ldg(a.sp_wr + (int64_t)q * M + t_sp);
-        else if (q == 9) w = 9 * Np + n;
-        else if (m & (1u << OPP(q))) w = (int64_t)OPP(q) * Np + n;
-        else w = (int64_t)q * Np + n + dI[1 + CX(q)] + dJ[1 + CY(q)] + dK[1 + CZ(q)];
-        lo[q] = (C)lam[w];
-    });
-    const double *du_loss = nullptr;
-    double dl[3];
-    if (A.seed && i == A.plane) {
-        const double *tg = A.target + 3 * ((int64_t)j * a.nz + k);
-        // stored velocity of the collision input
-        C rho = ST::shifted ? (C)1 : (C)0, jx = 0, jy = 0, jz = 0;
+    if (t < M) {
+        const int64_t Np = a.Np;
+        const int64_t n = __ldg(a.sp_node + t);
+        const int i = (int)(n / ((int64_t)a.ny * a.nz));
+        const int j = (int)((n / a.nz) % a.ny), k = (int)(n % a.nz);
+        const S *gin = (const S *)A.sp_in;
+        S *lam = (S *)A.lam;
+        C g[Q], lo[Q], li[Q];
         Unroll<0, Q>::run([&]<int q>() {
-            rho += g[q];
-            if (CX(q)) jx += (C)CX(q) * g[q];
-            if (CY(q)) jy += (C)CY(q) * g[q];
-            if (CZ(q)) jz += (C)CZ(q) * g[q];
+            g[q] = ST::template ld<q>(gin + (int64_t)q * M + t);
+            const int64_t w = PSTEP ? __ldg(a.sp_wr + (int64_t)q * M + t) : (int64_t)OPP(q) * Np + n;
+            lo[q] = (C)lam[w];
         });
-        const double u0 = (double)(jx / rho) + 0.5 * a.g[0], u1 = (double)(jy / rho) + 0.5 * a.g[1],
-                     u2 = (double)(jz / rho) + 0.5 * a.g[2];
-        dl[0] = 2.0 * (u0 - tg[0]); dl[1] = 2.0 * (u1 - tg[1]); dl[2] = 2.0 * (u2 - tg[2]);
-        du_loss = dl;
-    }
-    coll_adjoint<C, ST::shifted, SCH>(g, lo, (C)a.g[0], (C)a.g[1], (C)a.g[2], (C)a.w_e, (C)a.w_o, li, pg, du_loss);
-    if (special) {
-        const uint32_t info = __ldg(a.sp_info + t_sp);
+        const double *tg = nullptr;
+        const bool on_plane = SEED && i == A.plane;
+        if (on_plane) tg = A.target + 3 * ((int64_t)j * a.nz + k);
+        AdjSums<C, ST::shifted> sums;
+        adj_accumulate(sums, g, lo);
+        adj_finish<C, ST::shifted, SCH, SEED>(sums, lo, (C)a.g[0], (C)a.g[1], (C)a.g[2], (C)a.w_e, (C)a.w_o, pg, on_plane,
+                                             tg, a.g[0], a.g[1], a.g[2], [&]<int q>(C v) { li[q] = v; });
+        const uint32_t info = __ldg(a.sp_info + t);
         const uint32_t faces = (info >> SP_FACE_SHIFT) & 0x3Fu;
         // faces were applied in increasing order, so transpose in decreasing
         int slots[6], nf = 0;
@@ -305,76 +392,58 @@ __device__ __forceinline__ void adj_node(const AdjArgs &A, bool pstep, bool spec
             if (faces & (1u << fc)) slots[fc] = nf++;
         for (int fc = 5; fc >= 0; --fc) {
             if (!(faces & (1u << fc))) continue;
-            const double *bcd = a.sp_bc + (int64_t)(4 * slots[fc]) * M + t_sp;
+            const double *bcd = a.sp_bc + (int64_t)(4 * slots[fc]) * M + t;
             double du[3] = {0, 0, 0};
             zh_adjoint<C, ST::shifted>(fc, a.bc[fc], bcd[0], bcd[M], bcd[2 * (int64_t)M], bcd[3 * (int64_t)M], g,
                                        li, du);
+            // one boundary site per inlet (j, k): a plain add is race-free
             if (fc == 0 && a.bc[0] == BC_FIXED_VEL && A.grad_uin) A.grad_uin[(int64_t)j * a.nz + k] += du[0];
         }
+        Unroll<0, Q>::run([&]<int q>() {
+            const int64_t r = PSTEP ? __ldg(a.sp_rd + (int64_t)q * M + t) : (int64_t)q * Np + n;
+            lam[r] = (S)li[q];
+        });
     }
-    Unroll<0, Q>::run([&]<int q>() {
-        // adjoint of input q goes where the forward step read g_q
-        int64_t r;
-        if (!pstep) r = (int64_t)q * Np + n;
-        else if (special) r = __ldg(a.sp_rd + (int64_t)q * M + t_sp);
-        else if (q == 9) r = 9 * Np + n;
-        else if (m & (1u << q)) r = (int64_t)q * Np + n;
-        else r = (int64_t)OPP(q) * Np + n + dI[1 - CX(q)] + dJ[1 - CY(q)] + dK[1 - CZ(q)];
-        lam[r] = (S)li[q];
-    });
+}
+
+int adjoint_blocks(const StepArgs &a) { return a.nb_dense + (a.M + 127) / 128; }
+
+// One step of the reverse sweep: blocks [0, nb_dense) take the dense sites,
+// the rest the boundary sites (disjoint address sets, as in the forward step).
+template <class ST, int SCH, bool PSTEP, bool SEED, class IT>
+__global__ void __launch_bounds__(128, adj_min_blocks<ST, SEED>()) adjoint_step_kernel(const AdjArgs A) {
+    using C = typename ST::C;
+    C pg[5] = {0, 0, 0, 0, 0};
+    const int b = (int)blockIdx.x;
+    if (b < A.s.nb_dense) adjoint_dense_sites<ST, SCH, PSTEP, SEED, IT>(A, b, pg);
+    else adjoint_boundary_sites<ST, SCH, PSTEP, SEED>(A, b - A.s.nb_dense, pg);
+    block_sensitivities<C>(pg, A.part + 5 * (int64_t)b);
+}
+
+template <class ST, int SCH, bool PSTEP, bool SEED>
+int launch_adjoint_typed(const AdjArgs &A, cudaStream_t st) {
+    const StepArgs &a = A.s;
+    const int blocks = adjoint_blocks(a);
+    if (blocks == 0) return 0;
+    const dim3 blk(a.bx, a.by), grd(blocks);
+    if (a.Np * 19 > 0x7fffffffLL) adjoint_step_kernel<ST, SCH, PSTEP, SEED, int64_t><<<grd, blk, 0, st>>>(A);
+    else adjoint_step_kernel<ST, SCH, PSTEP, SEED, int32_t><<<grd, blk, 0, st>>>(A);
+    return (int)cudaGetLastError();
 }
 
 template <class ST, int SCH>
-__global__ void __launch_bounds__(128) adjoint_step_kernel(const AdjArgs A, int pstep) {
-    const StepArgs &a = A.s;
-    double pg[5] = {0, 0, 0, 0, 0};
-    const int b = (int)blockIdx.x;
-    const int tid = (int)(threadIdx.y * blockDim.x + threadIdx.x);
-    if (b < a.nb_dense) {
-        const int kb = b % a.kblocks, rb = b / a.kblocks;
-        const int row = rb * a.by + (int)threadIdx.y;
-        const int k = kb * a.bx + (int)threadIdx.x;
-        if (row < a.nx * a.ny && k < a.nz) {
-            const int64_t n = (int64_t)row * a.nz + k;
-            const uint32_t m = a.nmask[n];
-            if (!(m & MASK_SKIP)) adj_node<ST, SCH>(A, pstep != 0, false, n, 0, m, row / a.ny, row % a.ny, k, pg);
-        }
-    } else {
-        const int t = (b - a.nb_dense) * (int)(blockDim.x * blockDim.y) + tid;
-        if (t < a.M) {
-            const int64_t n = a.sp_node[t];
-            const int i = (int)(n / ((int64_t)a.ny * a.nz));
-            const int j = (int)((n / a.nz) % a.ny), k = (int)(n % a.nz);
-            adj_node<ST, SCH>(A, pstep != 0, true, n, t, 0u, i, j, k, pg);
-        }
-    }
-    // block sums of the parameter sensitivities, one atomic per block and component
-    __shared__ double sm[5][4];
-    const int lane = tid & 31, wid = tid >> 5;
-#pragma unroll
-    for (int c = 0; c < 5; ++c) {
-        double v = pg[c];
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-        if (lane == 0) sm[c][wid] = v;
-    }
-    __syncthreads();
-    if (tid < 5) {
-        const double v = sm[tid][0] + sm[tid][1] + sm[tid][2] + sm[tid][3];
-        if (v != 0.0) atomicAdd(A.grad + tid, v);
-    }
+int launch_adjoint_scheme(const AdjArgs &A, bool pstep, bool seed, cudaStream_t st) {
+    if (pstep) return seed ? launch_adjoint_typed<ST, SCH, true, true>(A, st) : launch_adjoint_typed<ST, SCH, true, false>(A, st);
+    return seed ? launch_adjoint_typed<ST, SCH, false, true>(A, st) : launch_adjoint_typed<ST, SCH, false, false>(A, st);
 }
 
-int launch_adjoint_step(const AdjArgs &A, int prec, int scheme, bool pstep, int blocks, cudaStream_t st) {
-    dim3 blk(A.s.bx, A.s.by), grd(blocks);
-    if (prec == PREC_FP64) {
-        if (scheme == SCH_TRT) adjoint_step_kernel<StoreF64, SCH_TRT><<<grd, blk, 0, st>>>(A, pstep);
-        else adjoint_step_kernel<StoreF64, SCH_BGK><<<grd, blk, 0, st>>>(A, pstep);
-    } else {
-        if (scheme == SCH_TRT) adjoint_step_kernel<StoreF32, SCH_TRT><<<grd, blk, 0, st>>>(A, pstep);
-        else adjoint_step_kernel<StoreF32, SCH_BGK><<<grd, blk, 0, st>>>(A, pstep);
-    }
-    return (int)cudaGetLastError();
+int launch_adjoint_step(const AdjArgs &A, int prec, int scheme, bool pstep, cudaStream_t st) {
+    const bool seed = A.seed != 0;
+    if (prec == PREC_FP64)
+        return scheme == SCH_TRT ? launch_adjoint_scheme<StoreF64, SCH_TRT>(A, pstep, seed, st)
+                                 : launch_adjoint_scheme<StoreF64, SCH_BGK>(A, pstep, seed, st);
+    return scheme == SCH_TRT ? launch_adjoint_scheme<StoreF32, SCH_TRT>(A, pstep, seed, st)
+                             : launch_adjoint_scheme<StoreF32, SCH_BGK>(A, pstep, seed, st);
 }
 
 } // namespace jlb

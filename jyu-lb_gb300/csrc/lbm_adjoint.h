@@ -1,4 +1,4 @@
-// lbm_adjoint.h -- arguments and launcher of the adjoint step kernel
+// lbm_adjoint.h -- arguments and launcher of the adjoint step kernels
 // (lbm_adjoint.cu).
 #pragma once
 #include <stdint.h>
@@ -9,15 +9,20 @@ namespace jlb {
 
 struct AdjArgs {
     StepArgs s;            // the forward step's geometry, tables and parameters
-    const void *gin;       // collision inputs of this step, [19][Np] (storage type)
+    const void *snap;      // AA state before this step, [19][Np] (storage type)
+    const void *sp_in;     // collision inputs of the boundary sites, [19][M]
     void *lam;             // adjoint AA array, [19][Np] (storage type)
     int seed;              // 1 on the step whose stored velocity enters the loss
     int plane;             // x index of the loss plane
     const double *target;  // (ny, nz, 3) target velocity on the plane
-    double *grad;          // [5] d/d we, d/d wo, d/d a_x, a_y, a_z (accumulated)
+    double *part;          // [adjoint_blocks][5] per-block sums of d/d we, d/d wo,
+                           // d/d a_x, a_y, a_z (accumulated over the sweep)
     double *grad_uin;      // [ny*nz] d/d u_x of the FIXED_VEL face 1X (accumulated)
 };
 
-int launch_adjoint_step(const AdjArgs &A, int prec, int scheme, bool pstep, int blocks, cudaStream_t st);
+// one step of the reverse sweep (one launch)
+int launch_adjoint_step(const AdjArgs &A, int prec, int scheme, bool pstep, cudaStream_t st);
+// number of per-block sensitivity slots the launches use
+int adjoint_blocks(const StepArgs &a);
 
 } // namespace jlb

@@ -69,8 +69,10 @@ struct StepArgs {
     const double *sp_bc;  // [8][M] Zou-He data (den, ux, uy, uz) x 2 faces
     void *sp_den;         // [M] previous-step density (compute type; rho-1 if shifted)
     int bc[6];            // face kinds (for the Zou-He variant)
-    void *tee;            // if set: collision inputs (after Zou-He) of every
-                          // fluid node, [19][Np] in the storage type (adjoint recompute)
+    void *fout;           // if set: the step writes its outputs here instead of
+                          // back into f (same element indices; adjoint recompute)
+    void *sp_tee;         // if set: collision inputs (after Zou-He) of the
+                          // boundary nodes, [19][M] in the storage type
 };
 
 // launch entry points, one per precision translation unit

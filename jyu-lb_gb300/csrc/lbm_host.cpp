@@ -110,7 +110,6 @@ struct jlb_solver {
     bool tma_p = true; // also for the pull-push step
     int tma_grid = 0;
     int *d_err = nullptr; // set by a kernel whose bounded wait timed out
-    void *tee = nullptr;  // adjoint recompute: where steps copy their collision inputs
     uint64_t args_version = 1, graph_version[2] = {0, 0};
 };
 
@@ -571,7 +570,6 @@ StepArgs make_args(const jlb_solver *s, int write_moments) {
     a.sp_rd = s->d_sp_rd; a.sp_wr = s->d_sp_wr;
     a.sp_lw = s->d_sp_lw; a.sp_bc = s->d_sp_bc;
     a.sp_den = s->d_sp_den;
-    a.tee = s->tee;
     for (int f = 0; f < 6; ++f) a.bc[f] = s->cfg.bc[f];
     return a;
 }
@@ -580,7 +578,7 @@ int launch_one(jlb_solver *s, const StepArgs &a, bool pstep) {
     const int blocks = a.nb_dense + (a.M + 127) / 128;
     const int nsb = (a.M + 127) / 128;
     int r;
-    if (s->use_tma && !s->tee && (s->tma_p || !pstep)) {
+    if (s->use_tma && !a.fout && !a.sp_tee && (s->tma_p || !pstep)) {
         const int ntiles = a.nb_dense; // one 128-site tile per dense block (bx = 128, by = 1)
         if (s->prec == PREC_FP32)
             r = launch_step_tma_fp32(a, s->cfg.rlx_scheme, pstep, s->accf, s->tma_grid, ntiles, nsb, s->d_err, s->st);
@@ -1506,13 +1504,23 @@ struct jlb_adjoint {
     double magic = 0.0;       // TRT magic parameter (<= 0: reference's 3/16)
     void *f0 = nullptr;       // initial populations
     std::vector<void *> ckpt; // populations before steps 0, K, 2K, ...
-    std::vector<void *> tee;  // collision inputs of the K steps of a segment
+    // recompute buffers, nsets sets of K: set p holds the states before the
+    // steps of a segment in snap[p*K + 1 .. p*K + K-1] (snap[p*K] is scratch)
+    // and their boundary-site collision inputs in sp_in[p][K][19][M]; with two
+    // sets the recompute of one segment overlaps the reverse sweep of the next
+    std::vector<void *> snap;
+    void *sp_in = nullptr;
+    int nsets = 0;
+    cudaStream_t st2 = nullptr; // recompute stream
     void *lam = nullptr;
-    double *d_target = nullptr, *d_grad = nullptr, *d_guin = nullptr;
+    double *d_target = nullptr, *d_part = nullptr, *d_guin = nullptr;
+    int nparts = 0;           // per-block sensitivity slots
     uint32_t steps = 0;
     double tau = 1.0;
     bool have_forward = false;
     size_t fbytes = 0;
+    std::vector<cudaEvent_t> ev; // forward pair, backward pair, then 4 per backward segment
+    double ms[4] = {0, 0, 0, 0};  // forward, recompute, reverse sweep, whole backward
     std::string err;
 };
 
@@ -1532,6 +1540,23 @@ int afail(jlb_adjoint *A, int code, const std::string &m) {
                          std::string(#call) + ": " + cudaGetErrorString(e_));                      \
     } while (0)
 
+// the first n timing events, created on first use
+cudaError_t adj_events(jlb_adjoint *A, size_t n) {
+    while (A->ev.size() < n) {
+        cudaEvent_t e;
+        const cudaError_t r = cudaEventCreate(&e);
+        if (r != cudaSuccess) return r;
+        A->ev.push_back(e);
+    }
+    return cudaSuccess;
+}
+
+float adj_elapsed(const jlb_adjoint *A, size_t i, size_t j) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, A->ev[i], A->ev[j]);
+    return ms;
+}
+
 // relaxation rates of relaxation time tau (jyulb/isothermal.pyx:274-287)
 void adj_rates(const jlb_adjoint *A, double tau, double &we, double &wo) {
     we = 1.0 / tau;
@@ -1547,9 +1572,11 @@ extern "C" {
 void jlb_adj_destroy(jlb_adjoint *A) {
     if (!A) return;
     if (A->s) cudaStreamSynchronize(A->s->st);
+    if (A->st2) { cudaStreamSynchronize(A->st2); cudaStreamDestroy(A->st2); }
     for (void *p : A->ckpt) if (p) cudaFree(p);
-    for (void *p : A->tee) if (p) cudaFree(p);
-    void *bufs[] = {A->f0, A->lam, A->d_target, A->d_grad, A->d_guin};
+    for (void *p : A->snap) if (p) cudaFree(p);
+    for (cudaEvent_t e : A->ev) cudaEventDestroy(e);
+    void *bufs[] = {A->f0, A->lam, A->sp_in, A->d_target, A->d_part, A->d_guin};
     for (void *p : bufs) if (p) cudaFree(p);
     if (A->s) jlb_destroy(A->s);
     delete A;
@@ -1567,6 +1594,9 @@ int jlb_adj_create(const jlb_config *cfg, const uint8_t *phase, int32_t loss_pla
     for (int f = 1; f < 6; ++f)
         if (cfg->bc[f] == JLB_FIXED_VEL)
             return afail(nullptr, JLB_ERR_UNSUPPORTED, "adjoint: FIXED_VEL is supported on face 1X only");
+    for (int f = 0; f < 6; ++f)
+        if (cfg->bc[f] == JLB_SYMMETRIC)
+            return afail(nullptr, JLB_ERR_UNSUPPORTED, "adjoint: SYMMETRIC faces are not supported");
     if (cfg->bc[0] == JLB_FIXED_VEL && cfg->bc[1] != JLB_PERIODIC && cfg->lat_size[0] == 1)
         return afail(nullptr, JLB_ERR_UNSUPPORTED, "adjoint: a one-site-thick domain with two Zou-He faces");
     if (loss_plane < 0 || loss_plane >= cfg->lat_size[0]) return afail(nullptr, JLB_ERR_INVALID_ARG, "loss plane out of range");
@@ -1595,8 +1625,14 @@ int jlb_adj_create(const jlb_config *cfg, const uint8_t *phase, int32_t loss_pla
     auto bail = [&](const char *m) { jlb_adj_destroy(A); return afail(nullptr, JLB_ERR_NOMEM, m); };
     if (cudaMalloc(&A->f0, A->fbytes) != cudaSuccess || cudaMalloc(&A->lam, A->fbytes) != cudaSuccess ||
         cudaMalloc(&A->d_target, 3 * sizeof(double) * (size_t)s->ny * s->nz) != cudaSuccess ||
-        cudaMalloc(&A->d_grad, 8 * sizeof(double)) != cudaSuccess ||
         cudaMalloc(&A->d_guin, sizeof(double) * (size_t)s->ny * s->nz) != cudaSuccess) {
+        cudaGetLastError();
+        return bail("adjoint state allocation failed");
+    }
+    A->nparts = adjoint_blocks(make_args(s, 0));
+    if (cudaMalloc(&A->d_part, 5 * sizeof(double) * (size_t)A->nparts) != cudaSuccess ||
+        (s->M > 0 && cudaMalloc(&A->sp_in, (size_t)2 * A->K * 19 * s->M * s->ssz) != cudaSuccess) ||
+        cudaStreamCreateWithFlags(&A->st2, cudaStreamNonBlocking) != cudaSuccess) {
         cudaGetLastError();
         return bail("adjoint state allocation failed");
     }
@@ -1638,9 +1674,10 @@ int jlb_adj_forward(jlb_adjoint *A, double tau, const double g[3], const double 
         ACK(cudaMemsetAsync(s->d_sp_den, 0, (size_t)M * s->csz, s->st));
     }
     // forward with checkpoints
+    ACK(adj_events(A, 2));
+    ACK(cudaEventRecord(A->ev[0], s->st));
     ACK(cudaMemcpyAsync(s->f, A->f0, A->fbytes, cudaMemcpyDeviceToDevice, s->st));
     s->parity = 0;
-    s->tee = nullptr;
     const int nseg = (int)((steps + A->K - 1) / A->K);
     while ((int)A->ckpt.size() < nseg) {
         void *p = nullptr;
@@ -1653,6 +1690,7 @@ int jlb_adj_forward(jlb_adjoint *A, double tau, const double g[3], const double 
         int r = run_steps(s, t1 - t0, t1 == steps);
         if (r) return afail(A, r, s->err);
     }
+    ACK(cudaEventRecord(A->ev[1], s->st));
     // stored velocity on the loss plane, and the loss
     const size_t plane_n = (size_t)s->ny * s->nz;
     const int64_t p0 = (int64_t)A->plane * s->ny * s->nz;
@@ -1671,6 +1709,7 @@ int jlb_adj_forward(jlb_adjoint *A, double tau, const double g[3], const double 
         }
     }
     ACK(cudaStreamSynchronize(s->st));
+    A->ms[0] = adj_elapsed(A, 0, 1);
     double L = 0.0;
     for (size_t m = 0; m < plane_n; ++m) {
         if (pm[m] & MASK_SOLID) continue;
@@ -1697,49 +1736,117 @@ int jlb_adj_backward(jlb_adjoint *A, double *dtau, double dg[3], double *duin) {
     if (!A->have_forward) return afail(A, JLB_ERR_STATE, "run jlb_adj_forward first");
     jlb_solver *s = A->s;
     const uint32_t steps = A->steps;
-    const int nseg = (int)((steps + A->K - 1) / A->K);
-    while ((int)A->tee.size() < A->K) {
-        void *p = nullptr;
-        ACK(cudaMalloc(&p, A->fbytes));
-        A->tee.push_back(p);
-    }
-    ACK(cudaMemsetAsync(A->lam, 0, A->fbytes, s->st));
-    ACK(cudaMemsetAsync(A->d_grad, 0, 8 * sizeof(double), s->st));
-    ACK(cudaMemsetAsync(A->d_guin, 0, sizeof(double) * (size_t)s->ny * s->nz, s->st));
-    const int blocks = make_args(s, 0).nb_dense + (s->M + 127) / 128;
-    for (int seg = nseg - 1; seg >= 0; --seg) {
-        const uint32_t t0 = (uint32_t)seg * A->K, t1 = std::min<uint32_t>(steps, t0 + A->K);
-        // recompute the segment, keeping every step's collision inputs
-        ACK(cudaMemcpyAsync(s->f, A->ckpt[seg], A->fbytes, cudaMemcpyDeviceToDevice, s->st));
-        s->parity = (int)(t0 & 1u);
-        for (uint32_t t = t0; t < t1; ++t) {
-            s->tee = A->tee[t - t0];
-            int r = launch_one(s, make_args(s, 0), s->parity == 0);
-            s->tee = nullptr;
-            if (r) return afail(A, r, s->err);
-            s->parity ^= 1;
+    const int K = A->K;
+    const int nseg = (int)((steps + K - 1) / K);
+    // one buffer set, a second when memory allows (and there is a next segment)
+    const int want = nseg > 1 ? 2 : 1;
+    while (A->nsets < want) {
+        std::vector<void *> set;
+        bool ok = true;
+        for (int i = 0; i < K && ok; ++i) {
+            void *p = nullptr;
+            ok = cudaMalloc(&p, A->fbytes) == cudaSuccess;
+            if (ok) set.push_back(p);
         }
-        // reverse sweep over the segment
+        if (!ok) {
+            cudaGetLastError();
+            for (void *p : set) cudaFree(p);
+            if (A->nsets == 0) return afail(A, JLB_ERR_NOMEM, "adjoint recompute buffers");
+            break;
+        }
+        A->snap.insert(A->snap.end(), set.begin(), set.end());
+        ++A->nsets;
+    }
+    const int nsets = std::min(A->nsets, want);
+    ACK(adj_events(A, 4 + 4 * (size_t)nseg));
+    cudaEvent_t *ev = A->ev.data();
+    cudaStream_t st = s->st, st2 = A->st2;
+    ACK(cudaEventRecord(ev[2], st));
+    ACK(cudaMemsetAsync(A->lam, 0, A->fbytes, st));
+    ACK(cudaMemsetAsync(A->d_part, 0, 5 * sizeof(double) * (size_t)A->nparts, st));
+    ACK(cudaMemsetAsync(A->d_guin, 0, sizeof(double) * (size_t)s->ny * s->nz, st));
+    ACK(cudaStreamWaitEvent(st2, ev[2], 0)); // checkpoints of the forward run are complete
+    const size_t sp_step = (size_t)19 * s->M * s->ssz; // bytes of one step's boundary-site inputs
+    auto seg_ev = [&](int seg) { return ev + 4 + 4 * (size_t)seg; }; // rc start, rc end, rv start, rv end
+    auto range = [&](int seg, uint32_t &t0, uint32_t &t1) {
+        t0 = (uint32_t)seg * K;
+        t1 = std::min<uint32_t>(steps, t0 + K);
+    };
+    auto state_before = [&](int seg, uint32_t t) -> void * {
+        const uint32_t t0 = (uint32_t)seg * K;
+        return t == t0 ? A->ckpt[seg] : A->snap[(size_t)(seg % nsets) * K + (t - t0)];
+    };
+    auto sp_in_of = [&](int seg, uint32_t t) -> void * {
+        if (s->M == 0) return nullptr;
+        return (char *)A->sp_in + ((size_t)(seg % nsets) * K + (t - (uint32_t)seg * K)) * sp_step;
+    };
+    // recompute a segment out of place on st2; its last step's outputs are not
+    // needed, so that step runs the boundary sites only (into the scratch slot)
+    auto recompute = [&](int seg) -> int {
+        uint32_t t0, t1;
+        range(seg, t0, t1);
+        ACK(cudaEventRecord(seg_ev(seg)[0], st2));
+        for (uint32_t t = t0; t < t1; ++t) {
+            StepArgs a = make_args(s, 0);
+            a.f = state_before(seg, t);
+            a.fout = t + 1 < t1 ? state_before(seg, t + 1) : A->snap[(size_t)(seg % nsets) * K];
+            a.sp_tee = sp_in_of(seg, t);
+            if (t + 1 == t1) a.nb_dense = 0;
+            if (a.nb_dense == 0 && a.M == 0) continue;
+            const int blocks = a.nb_dense + (a.M + 127) / 128;
+            const bool pstep = (t & 1u) == 0;
+            const int r = s->prec == PREC_FP64 ? launch_step_fp64(a, s->cfg.rlx_scheme, pstep, s->accf, blocks, st2)
+                                               : launch_step_fp32(a, s->cfg.rlx_scheme, pstep, s->accf, blocks, st2);
+            if (r) return afail(A, JLB_ERR_CUDA, std::string("recompute step: ") + cudaGetErrorString((cudaError_t)r));
+            ++s->launches;
+        }
+        ACK(cudaEventRecord(seg_ev(seg)[1], st2));
+        return JLB_OK;
+    };
+    int r = recompute(nseg - 1);
+    if (r) return r;
+    for (int seg = nseg - 1; seg >= 0; --seg) {
+        uint32_t t0, t1;
+        range(seg, t0, t1);
+        ACK(cudaStreamWaitEvent(st, seg_ev(seg)[1], 0));
+        ACK(cudaEventRecord(seg_ev(seg)[2], st));
         for (int64_t t = (int64_t)t1 - 1; t >= (int64_t)t0; --t) {
             AdjArgs a{};
             a.s = make_args(s, 0);
-            a.s.tee = nullptr;
-            a.gin = A->tee[t - t0];
+            a.snap = state_before(seg, (uint32_t)t);
+            a.sp_in = sp_in_of(seg, (uint32_t)t);
             a.lam = A->lam;
             a.seed = (uint32_t)t == steps - 1;
             a.plane = A->plane;
             a.target = A->d_target;
-            a.grad = A->d_grad;
+            a.part = A->d_part;
             a.grad_uin = A->d_guin;
-            const int r = launch_adjoint_step(a, s->prec, s->cfg.rlx_scheme, (t & 1) == 0, blocks, s->st);
+            r = launch_adjoint_step(a, s->prec, s->cfg.rlx_scheme, (t & 1) == 0, st);
             if (r) return afail(A, JLB_ERR_CUDA, std::string("adjoint step: ") + cudaGetErrorString((cudaError_t)r));
-            ++s->launches;
+            s->launches += 2;
+        }
+        ACK(cudaEventRecord(seg_ev(seg)[3], st));
+        if (seg > 0) {
+            // the buffer set of segment seg-1 was last read by the sweep of
+            // segment seg-1+nsets
+            if (seg - 1 + nsets < nseg) ACK(cudaStreamWaitEvent(st2, seg_ev(seg - 1 + nsets)[3], 0));
+            if ((r = recompute(seg - 1))) return r;
         }
     }
-    double gr[8];
-    ACK(cudaMemcpyAsync(gr, A->d_grad, 8 * sizeof(double), cudaMemcpyDeviceToHost, s->st));
-    if (duin) ACK(cudaMemcpyAsync(duin, A->d_guin, sizeof(double) * (size_t)s->ny * s->nz, cudaMemcpyDeviceToHost, s->st));
-    ACK(cudaStreamSynchronize(s->st));
+    ACK(cudaEventRecord(ev[3], st));
+    std::vector<double> part(5 * (size_t)A->nparts);
+    ACK(cudaMemcpyAsync(part.data(), A->d_part, part.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+    if (duin) ACK(cudaMemcpyAsync(duin, A->d_guin, sizeof(double) * (size_t)s->ny * s->nz, cudaMemcpyDeviceToHost, st));
+    ACK(cudaStreamSynchronize(st));
+    double gr[5] = {0, 0, 0, 0, 0};
+    for (int b = 0; b < A->nparts; ++b)
+        for (int c = 0; c < 5; ++c) gr[c] += part[5 * (size_t)b + c];
+    A->ms[1] = A->ms[2] = 0.0;
+    for (int seg = 0; seg < nseg; ++seg) {
+        A->ms[1] += adj_elapsed(A, 4 + 4 * (size_t)seg, 5 + 4 * (size_t)seg);
+        A->ms[2] += adj_elapsed(A, 6 + 4 * (size_t)seg, 7 + 4 * (size_t)seg);
+    }
+    A->ms[3] = adj_elapsed(A, 2, 3);
     // chain rule to tau: we = 1/tau, wo(tau) from the magic parameter
     double we, wo;
     adj_rates(A, A->tau, we, wo);
@@ -1753,6 +1860,12 @@ int jlb_adj_backward(jlb_adjoint *A, double *dtau, double dg[3], double *duin) {
         else *dtau = (gr[0] + gr[1]) * (-we * we);
     }
     if (dg) for (int d = 0; d < 3; ++d) dg[d] = gr[2 + d];
+    return JLB_OK;
+}
+
+int jlb_adj_timers(const jlb_adjoint *A, double out[4]) {
+    if (!A || !out) return JLB_ERR_INVALID_ARG;
+    for (int i = 0; i < 4; ++i) out[i] = A->ms[i];
     return JLB_OK;
 }
 

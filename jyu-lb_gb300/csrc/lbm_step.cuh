@@ -154,10 +154,6 @@ __device__ __forceinline__ void dense_node(const StepArgs &a, int b) {
         }
         fv[q] = ST::template ld<q>(f + e);
     });
-    if (a.tee) {
-        S *tee = (S *)a.tee;
-        Unroll<0, Q>::run([&]<int q>() { ST::template st<q>(tee + ((IT)q * Np + n), fv[q]); });
-    }
 
     C ax, ay, az;
     if (ACCF) {
@@ -173,10 +169,11 @@ __device__ __forceinline__ void dense_node(const StepArgs &a, int b) {
 
     // scatter: a population heading into a solid is stored back into this
     // node's opposite slot
+    S *fo = a.fout ? (S *)a.fout : f;
     Unroll<0, Q>::run([&]<int q>() {
         IT e;
         if (!PSTEP) {
-            ST::template st<OPP(q)>(f + ((IT)OPP(q) * Np + n), fv[q]);
+            ST::template st<OPP(q)>(fo + ((IT)OPP(q) * Np + n), fv[q]);
             return;
         }
         if (q == 9) {
@@ -187,7 +184,7 @@ __device__ __forceinline__ void dense_node(const StepArgs &a, int b) {
             const IT e_bb = (IT)OPP(q) * Np + n;
             e = (m & (1u << OPP(q))) ? e_bb : e_reg;
         }
-        ST::template st<q>(f + e, fv[q]);
+        ST::template st<q>(fo + e, fv[q]);
     });
 
     if (a.write_moments) {
@@ -238,9 +235,9 @@ __device__ __forceinline__ void special_node(const StepArgs &a, int b) {
             }
         }
     }
-    if (a.tee) {
-        S *tee = (S *)a.tee;
-        Unroll<0, Q>::run([&]<int q>() { ST::template st<q>(tee + ((int64_t)q * Np + n), fv[q]); });
+    if (a.sp_tee) {
+        S *tee = (S *)a.sp_tee;
+        Unroll<0, Q>::run([&]<int q>() { ST::template st<q>(tee + ((int64_t)q * M + t), fv[q]); });
     }
 
     C ax, ay, az;
@@ -255,12 +252,13 @@ __device__ __forceinline__ void special_node(const StepArgs &a, int b) {
     C ux, uy, uz;
     const C rho = PH::collide(fv, ax, ay, az, (C)a.w_e, (C)a.w_o, ux, uy, uz);
 
+    S *fo = a.fout ? (S *)a.fout : f;
     Unroll<0, Q>::run([&]<int q>() {
         if (PSTEP) {
             const int64_t addr = __ldg(a.sp_wr + (int64_t)q * M + t);
-            ST::template st<q>(f + addr, fv[q]);
+            ST::template st<q>(fo + addr, fv[q]);
         } else {
-            ST::template st<OPP(q)>(f + OPP(q) * Np + n, fv[q]);
+            ST::template st<OPP(q)>(fo + OPP(q) * Np + n, fv[q]);
         }
     });
     spden[t] = rho;

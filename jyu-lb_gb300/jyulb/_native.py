@@ -28,7 +28,7 @@ EXPORTED_SYMBOLS = (
     "jlb_transfer_bytes", "jlb_host_timers",
     "jlb_last_error", "jlb_batch_create", "jlb_batch_destroy", "jlb_batch_step", "jlb_batch_moments",
     "jlb_batch_populations", "jlb_batch_info", "jlb_batch_domain_fluid", "jlb_batch_last_error",
-    "jlb_adj_create", "jlb_adj_destroy", "jlb_adj_forward", "jlb_adj_backward", "jlb_adj_last_error",
+    "jlb_adj_create", "jlb_adj_destroy", "jlb_adj_forward", "jlb_adj_backward", "jlb_adj_timers", "jlb_adj_last_error",
     "jlb_build_info",
 )
 
@@ -111,6 +111,7 @@ def load() -> ctypes.CDLL:
         "jlb_adj_forward": (ctypes.c_int, [vp, ctypes.c_double, dp, dp, ctypes.c_double, ctypes.c_uint32, dp, dp,
                                            dp]),
         "jlb_adj_backward": (ctypes.c_int, [vp, dp, dp, dp]),
+        "jlb_adj_timers": (ctypes.c_int, [vp, dp]),
         "jlb_adj_last_error": (ctypes.c_char_p, [vp]),
         "jlb_build_info": (ctypes.c_char_p, []),
     }

@@ -83,6 +83,14 @@ class ChannelProblem:
         return float(dtau.value), dg, duin
 
 
+    def timers(self):
+        """Device milliseconds of the last runs: forward, recompute, reverse
+        sweep, whole backward."""
+        out = np.zeros(4)
+        self._check(self._lib.jlb_adj_timers(self._h, _native.dptr(out)))
+        return {"forward": out[0], "recompute": out[1], "reverse": out[2], "backward": out[3]}
+
+
 def loss_fn(problem, tau, g, uin, target, steps, rho_out=1.0):
     """L(tau, g, uin) as a differentiable torch scalar (torch tensors in,
     gradients from the adjoint)."""

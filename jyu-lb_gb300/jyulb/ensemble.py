@@ -104,7 +104,7 @@ class Ensemble:
         out = (ctypes.c_int64 * 8)()
         self._check(self._lib.jlb_batch_info(self._h, out))
         return {'sites': out[0], 'fluid_sites': out[1], 'block': out[2], 'tiles': out[3],
-                'launches': out[4], 'tune_ns_per_step': {64: out[5], 128: out[6], 256: out[7]}}
+                'launches': out[4], 'tune_us_per_step': {64: out[5], 128: out[6], 256: out[7]}}
 
     def fluid_sites(self, d):
         return int(self._lib.jlb_batch_domain_fluid(self._h, d))

@@ -25,7 +25,7 @@ def setup(seed=0, shape=(16, 10, 6), r=2.0):
     return phase, uin, target
 
 
-def torch_grads(phase, tau, g, uin, target, steps, plane, scheme, magic):
+def torch_grads(phase, tau, g, uin, target, steps, plane, scheme, magic, zwall=False):
     import torch
 
     from torch_lbm import run
@@ -33,7 +33,7 @@ def torch_grads(phase, tau, g, uin, target, steps, plane, scheme, magic):
     t_tau = torch.tensor(tau, dtype=torch.float64, requires_grad=True)
     t_g = torch.tensor(g, dtype=torch.float64, requires_grad=True)
     t_uin = torch.tensor(uin, dtype=torch.float64, requires_grad=True)
-    u = run(phase, t_tau, t_g, t_uin, steps, magic=magic, scheme=scheme)
+    u = run(phase, t_tau, t_g, t_uin, steps, magic=magic, scheme=scheme, periodic=(False, False, not zwall))
     fl = torch.from_numpy(phase[plane] != 0)
     d = u[:, plane].permute(1, 2, 0) - torch.tensor(target)
     L = (d[fl] ** 2).sum()
@@ -41,22 +41,23 @@ def torch_grads(phase, tau, g, uin, target, steps, plane, scheme, magic):
     return float(L.detach()), float(t_tau.grad), t_g.grad.numpy(), t_uin.grad.numpy()
 
 
-@pytest.mark.parametrize("scheme", ["TRT", "BGK"])
-def test_fp64_adjoint_matches_torch_autograd(scheme):
+@pytest.mark.parametrize("scheme,zwall", [("TRT", False), ("BGK", False), ("TRT", True)])
+def test_fp64_adjoint_matches_torch_autograd(scheme, zwall):
     from jyulb.adjoint import ChannelProblem
-    from jyulb.defs import BGK, FP64, TRT
+    from jyulb.defs import BGK, FIXED_DEN, FIXED_VEL, FP64, PERIODIC, TRT, WALL
 
     phase, uin, target = setup(1)
-    tau, g, steps, plane = 0.8, np.array([1e-5, 2e-6, 0.0]), 30, 12
+    tau, g, steps, plane = 0.8, np.array([1e-5, 2e-6, 1e-6 if zwall else 0.0]), 30, 12
     magic = 0.25 if scheme == "TRT" else None
-    p = ChannelProblem(phase, rlx_scheme=TRT if scheme == "TRT" else BGK, precision=FP64, trt_magic=magic,
-                       loss_plane=plane, checkpoint_every=7)
+    zb = WALL if zwall else PERIODIC
+    p = ChannelProblem(phase, bc=[FIXED_VEL, FIXED_DEN, WALL, WALL, zb, zb], rlx_scheme=TRT if scheme == "TRT" else BGK,
+                       precision=FP64, trt_magic=magic, loss_plane=plane, checkpoint_every=7)
     L, _ = p.forward(tau, g, uin, steps, target)
     dtau, dg, duin = p.backward()
-    Lt, dtau_t, dg_t, duin_t = torch_grads(phase, tau, g, uin, target, steps, plane, scheme, magic)
+    Lt, dtau_t, dg_t, duin_t = torch_grads(phase, tau, g, uin, target, steps, plane, scheme, magic, zwall)
     assert abs(L - Lt) <= 1e-10 * abs(Lt)
     assert abs(dtau - dtau_t) <= 1e-8 * abs(dtau_t)
-    np.testing.assert_allclose(dg[:2], dg_t[:2], rtol=1e-8)
+    np.testing.assert_allclose(dg[:3 if zwall else 2], dg_t[:3 if zwall else 2], rtol=1e-8)
     np.testing.assert_allclose(duin, duin_t, rtol=1e-7, atol=1e-9 * np.abs(duin_t).max())
 
 
