@@ -119,6 +119,17 @@ int jlb_set_populations(jlb_solver *s, const double *f);
  * out[7] = number of non-finite den/u values found. */
 int jlb_reduce(jlb_solver *s, double out[8]);
 
+/* Flow information of the last moment-writing step, as the C++ executable's
+ * IsothermalSolver::calc_flow_info (include/solver/solver.cpp:64-129)
+ * computes it over fluid sites, in the column order of its .evol file
+ * (source/isothermal/jyu_lb_isothermal.cpp:21-56):
+ *   out[0] sum den, out[1..3] sum den*u, out[4] sum den*|u|,
+ *   out[5..7] mean u, out[8] mean |u|, out[9] max |u|, out[10] max den,
+ *   out[11] min den.
+ * The extremes start from ref_den (density) and 0 (speed), as there.  Sums
+ * are FP64 on the GPU in a fixed order. */
+int jlb_flow_info(jlb_solver *s, double ref_den, double out[12]);
+
 /* Allocation-free variant of jlb_reduce, for callers that cannot call
  * cudaMalloc (code inside another framework's memory pool, hosts that forbid
  * allocation after start-up, drivers that budget device memory themselves).

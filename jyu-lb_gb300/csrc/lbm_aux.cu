@@ -299,6 +299,84 @@ __global__ void reduce_final_kernel(const double *partial, int nblocks, double *
 }
 
 // ---------------------------------------------------------------------------
+// flow information (the C++ executable's IsothermalSolver::calc_flow_info,
+// include/solver/solver.cpp:64-129): over fluid sites, sums of den, j = den u,
+// |j| = den |u|, u and |u|, and the extremes max den, min den, max |u|.  The
+// extremes start from the reference density and 0 as there.  Per-block
+// partials, then one block combines them in index order.
+// partial layout per block: [0..8] sums (den, jx, jy, jz, |j|, ux, uy, uz,
+// |u|), [9] max den, [10] min den, [11] max |u|
+// ---------------------------------------------------------------------------
+constexpr int FI_VALUES = 12;
+
+template <class C, bool SHIFTED>
+__global__ void __launch_bounds__(RED_THREADS) flowinfo_partial_kernel(AuxGeom g, const uint32_t *nmask,
+                                                                       const C *den, const C *ux, const C *uy,
+                                                                       const C *uz, double ref_den,
+                                                                       double *partial) {
+    double acc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    double dmax = ref_den, dmin = ref_den, umax = 0.0;
+    for (int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; n < g.N;
+         n += (int64_t)gridDim.x * blockDim.x) {
+        if (nmask[n] & MASK_SOLID) continue;
+        const double d = SHIFTED ? 1.0 + (double)den[n] : (double)den[n];
+        const double u0 = (double)ux[n], u1 = (double)uy[n], u2 = (double)uz[n];
+        const double um = sqrt(u0 * u0 + u1 * u1 + u2 * u2);
+        acc[0] += d;
+        acc[1] += d * u0; acc[2] += d * u1; acc[3] += d * u2;
+        acc[4] += d * um;
+        acc[5] += u0; acc[6] += u1; acc[7] += u2;
+        acc[8] += um;
+        dmax = fmax(dmax, d);
+        dmin = fmin(dmin, d);
+        umax = fmax(umax, um);
+    }
+    __shared__ double sm[FI_VALUES][RED_THREADS / 32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int c = 0; c < 9; ++c) {
+        double v = acc[c];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (lane == 0) sm[c][wid] = v;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        dmax = fmax(dmax, __shfl_down_sync(0xffffffffu, dmax, o));
+        dmin = fmin(dmin, __shfl_down_sync(0xffffffffu, dmin, o));
+        umax = fmax(umax, __shfl_down_sync(0xffffffffu, umax, o));
+    }
+    if (lane == 0) { sm[9][wid] = dmax; sm[10][wid] = dmin; sm[11][wid] = umax; }
+    __syncthreads();
+    if (threadIdx.x < FI_VALUES) {
+        const int c = threadIdx.x;
+        double v = sm[c][0];
+        for (int w = 1; w < RED_THREADS / 32; ++w) {
+            const double x = sm[c][w];
+            v = c < 9 ? v + x : (c == 10 ? fmin(v, x) : fmax(v, x));
+        }
+        partial[(int64_t)blockIdx.x * FI_VALUES + c] = v;
+    }
+}
+
+__global__ void flowinfo_final_kernel(const double *partial, int nblocks, double *out) {
+    const int c = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (c >= FI_VALUES) return;
+    const bool is_sum = c < 9, is_min = c == 10;
+    double v = is_sum ? 0.0 : partial[c];
+    for (int b = lane; b < nblocks; b += 32) {
+        const double x = partial[(int64_t)b * FI_VALUES + c];
+        v = is_sum ? v + x : (is_min ? fmin(v, x) : fmax(v, x));
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const double x = __shfl_down_sync(0xffffffffu, v, o);
+        v = is_sum ? v + x : (is_min ? fmin(v, x) : fmax(v, x));
+    }
+    if (lane == 0) out[c] = v;
+}
+
+// ---------------------------------------------------------------------------
 // host-callable launchers
 // ---------------------------------------------------------------------------
 static inline unsigned nblk(int64_t n, int t) { return (unsigned)((n + t - 1) / t); }
@@ -375,6 +453,21 @@ int aux_reduce(int prec, const AuxGeom &g, const uint32_t *nmask, const void *de
         reduce_partial_kernel<float, true><<<nblocks, RED_THREADS, 0, st>>>(
             g, nmask, (const float *)den, (const float *)ux, (const float *)uy, (const float *)uz, partial);
     reduce_final_kernel<<<1, 256, 0, st>>>(partial, nblocks, out);
+    return (int)cudaGetLastError();
+}
+
+int aux_flow_info(int prec, const AuxGeom &g, const uint32_t *nmask, const void *den, const void *ux,
+                  const void *uy, const void *uz, double ref_den, double *partial, int nblocks, double *out,
+                  cudaStream_t st) {
+    if (prec == PREC_FP64)
+        flowinfo_partial_kernel<double, false><<<nblocks, RED_THREADS, 0, st>>>(
+            g, nmask, (const double *)den, (const double *)ux, (const double *)uy, (const double *)uz, ref_den,
+            partial);
+    else
+        flowinfo_partial_kernel<float, true><<<nblocks, RED_THREADS, 0, st>>>(
+            g, nmask, (const float *)den, (const float *)ux, (const float *)uy, (const float *)uz, ref_den,
+            partial);
+    flowinfo_final_kernel<<<1, 32 * FI_VALUES, 0, st>>>(partial, nblocks, out);
     return (int)cudaGetLastError();
 }
 

@@ -70,6 +70,7 @@ struct jlb_solver {
     void *acc = nullptr;
     double *red_partial = nullptr, *red_out = nullptr;
     int red_blocks = 0;
+    double *fi_partial = nullptr, *fi_out = nullptr; // flow information (allocated on first use)
     // boundary-node tables (device)
     int M = 0, Mcap = 0;
     int64_t *d_sp_node = nullptr, *d_sp_rd = nullptr, *d_sp_wr = nullptr;
@@ -834,7 +835,7 @@ void jlb_destroy(jlb_solver *s) {
     drop_graphs(s);
     void *bufs[] = {s->f, s->nmask, s->ncls, s->mom[0], s->mom[1], s->mom[2], s->mom[3], s->acc, s->red_partial,
                     s->red_out, s->d_sp_node, s->d_sp_info, s->d_sp_rd, s->d_sp_wr, s->d_sp_lw, s->d_sp_bc,
-                    s->d_sp_den, s->d_err};
+                    s->d_sp_den, s->d_err, s->fi_partial, s->fi_out};
     for (void *p : bufs)
         if (p) cudaFree(p);
     if (s->pinned) cudaFreeHost(s->pinned);
@@ -1034,6 +1035,32 @@ int jlb_reduce(jlb_solver *s, double out[8]) {
     CK(cudaMemcpyAsync(out, s->red_out, 8 * sizeof(double), cudaMemcpyDeviceToHost, s->st));
     CK(cudaStreamSynchronize(s->st));
     if (out[7] != 0.0) return fail(s, JLB_ERR_NUMERIC, "non-finite density or velocity found");
+    return JLB_OK;
+}
+
+int jlb_flow_info(jlb_solver *s, double ref_den, double out[12]) {
+    if (!s || !out) return fail(s, JLB_ERR_INVALID_ARG, "NULL argument");
+    if (!s->init_done) return fail(s, JLB_ERR_STATE, "finalize_init has not been called");
+    if (!s->fi_partial) {
+        CK(cudaMalloc(&s->fi_partial, (size_t)12 * s->red_blocks * sizeof(double)));
+        CK(cudaMalloc(&s->fi_out, 12 * sizeof(double)));
+    }
+    CKR(aux_flow_info(s->prec, s->geom, s->nmask, s->mom[0], s->mom[1], s->mom[2], s->mom[3], ref_den,
+                      s->fi_partial, s->red_blocks, s->fi_out, s->st));
+    s->launches += 2;
+    double v[12];
+    CK(cudaMemcpyAsync(v, s->fi_out, sizeof(v), cudaMemcpyDeviceToHost, s->st));
+    CK(cudaStreamSynchronize(s->st));
+    // order of the .evol columns 3-14 (source/isothermal/jyu_lb_isothermal.cpp:21-56)
+    out[0] = v[0];
+    out[1] = v[1]; out[2] = v[2]; out[3] = v[3];
+    out[4] = v[4];
+    const double cff = s->nfluid > 0 ? 1.0 / (double)s->nfluid : 0.0;
+    out[5] = cff * v[5]; out[6] = cff * v[6]; out[7] = cff * v[7];
+    out[8] = cff * v[8];
+    out[9] = v[11];
+    out[10] = v[9];
+    out[11] = v[10];
     return JLB_OK;
 }
 

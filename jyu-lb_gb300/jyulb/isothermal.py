@@ -338,6 +338,22 @@ class Solver:
             self._raise(rc)
         return {'mass': out[0], 'momentum': out[1:4].copy(), 'vel_sum': out[4:7].copy()}
 
+    FLOW_INFO_KEYS = ('tot_den', 'tot_jx', 'tot_jy', 'tot_jz', 'tot_j2', 'ave_ux', 'ave_uy', 'ave_uz', 'ave_u2',
+                      'max_u2', 'max_den', 'min_den')
+
+    def flow_info(self, ref_den=1.0):
+        """Flow information of the last step, as the C++ executable's
+        IsothermalSolver::calc_flow_info (include/solver/solver.cpp:64-129):
+        sums of den, den*u and den*|u|, means of u and |u|, max |u| and the
+        density extremes over fluid sites (``*_u2`` are speeds |u|, as
+        there).  Computed in FP64 on the GPU."""
+        self._need_init()
+        out = np.zeros(12)
+        rc = self._lib.jlb_flow_info(self._h, float(ref_den), _native.dptr(out))
+        if rc != _native.JLB_OK:
+            self._raise(rc)
+        return dict(zip(self.FLOW_INFO_KEYS, (float(v) for v in out)))
+
     @property
     def kernel_launches(self):
         return int(self._lib.jlb_kernel_launches(self._h))
