@@ -367,15 +367,18 @@ def run_porous(args):
     torch.cuda.set_device(0)
     st = torch.cuda.Stream()
     t0 = time.perf_counter()
-    phase, por = porous_geometry()
+    shape = tuple(max(32, int(n * args.porous_scale)) for n in POROUS_SHAPE)
+    phase, por = porous_geometry(shape=shape)
     geom_s = time.perf_counter() - t0
     steps = args.porous_steps
     bc = np.array([PERIODIC, PERIODIC, WALL, WALL, PERIODIC, PERIODIC], dtype=np.int32)
     peak, peak_kind = measured_peak()
     res, vel = {}, {}
     nsites = phase.size
-    for name, prec, bps in (("fp32", FP32, BYTES_FP32), ("fp16", FP16, 76), ("fp64", FP64, BYTES_FP64)):
-        s = Solver(np.array(POROUS_SHAPE, dtype=np.int32), REGULARIZATION, (0.7 - 0.5) / 3.0,
+    runs = [r for r in (("fp32", FP32, BYTES_FP32), ("fp16", FP16, 76), ("fp64", FP64, BYTES_FP64))
+            if r[0] in args.porous_precisions.split(",")]
+    for name, prec, bps in runs:
+        s = Solver(np.array(shape, dtype=np.int32), REGULARIZATION, (0.7 - 0.5) / 3.0,
                    np.array([5e-6, 0.0, 0.0]), bc, precision=prec, stream=st.cuda_stream)
         s.get_phase()[:] = phase
         nf = s.finalize_init()
@@ -400,6 +403,8 @@ def run_porous(args):
         del s
     fl = phase != 0
     for name in ("fp32", "fp16"):
+        if name not in res or "fp64" not in res:
+            continue
         d64 = res["fp64"]["darcy_flux"]
         res[name]["darcy_rel_err_vs_fp64"] = abs(res[name]["darcy_flux"] - d64) / abs(d64)
         res[name]["vel_rel_l2_vs_fp64"] = float(np.linalg.norm(vel[name][fl] - vel["fp64"][fl]) /
@@ -409,7 +414,7 @@ def run_porous(args):
         "value": res["fp32"]["mlups"], "unit": "MLUPS", "n_gpus": 1, "steps": steps, "warmup": 0,
         "ms_per_step": res["fp32"]["ms_per_step"], "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "porous channel 384x256x256, regularized tau=0.7, gx=5e-6, seeded spheres r=8 "
+        "config": {"workload": f"porous channel {shape[0]}x{shape[1]}x{shape[2]}, regularized tau=0.7, gx=5e-6, seeded spheres r=8 "
                                "(jittered lattice, random order) to porosity 0.6, periodic x/z, walls at the y ends",
                    "porosity": round(por, 5), "fluid_sites": int(fl.sum()), "geometry_s": round(geom_s, 1),
                    "l2_policy": "inputs larger than L2 (FP16 populations 1.9 GB), no flush"},
@@ -607,6 +612,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="cavity", choices=["cavity", "ensemble", "adjoint", "porous"])
     ap.add_argument("--porous-steps", type=int, default=5000)
+    ap.add_argument("--porous-scale", type=float, default=1.0)
+    ap.add_argument("--porous-precisions", default="fp32,fp16,fp64")
     ap.add_argument("--adj-steps", type=int, default=2000)
     ap.add_argument("--adj-reps", type=int, default=3)
     ap.add_argument("--adj-ckpt", type=int, default=50)

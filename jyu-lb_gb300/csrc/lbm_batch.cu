@@ -15,6 +15,17 @@
 
 namespace jlb {
 
+// floor(l / d) and the remainder for 0 <= l < 2^23, from a float reciprocal:
+// the product is within 1 of l/d, so one correction step either way is exact
+__device__ __forceinline__ int32_t split_div(int32_t l, int32_t d, float inv, int32_t &rem) {
+    int32_t q = (int32_t)((float)l * inv);
+    int32_t r = l - q * d;
+    if (r < 0) { --q; r += d; }
+    else if (r >= d) { ++q; r -= d; }
+    rem = r;
+    return q;
+}
+
 template <int SCH, bool PSTEP, int BLOCK>
 __global__ void __launch_bounds__(BLOCK, (BLOCK >= 256 ? 3 : BLOCK >= 128 ? 6 : 12))
     lbm_batch_kernel(const BatchArgs a) {
@@ -29,31 +40,34 @@ __global__ void __launch_bounds__(BLOCK, (BLOCK >= 256 ? 3 : BLOCK >= 128 ? 6 : 
     const int32_t n = D.off + l;
     const uint8_t cls = __ldg(a.ncls + n);
     if (cls == BCLS_SOLID) return;
-    const int64_t Np = a.Np; // 19 * Np exceeds 2^31 for large ensembles
-    float *__restrict__ f = a.f;
+    // rows of 19 * Np exceed 2^31 elements for large ensembles; each row
+    // itself is indexed by a 32-bit site
     const uint32_t m = (PSTEP && cls != BCLS_PLAIN) ? __ldg(a.nmask + n) : 0u;
     const uint32_t mv = (cls == BCLS_MOVING) ? __ldg(a.mmask + n) : 0u;
     C fv[Q];
     int32_t dI[3], dJ[3], dK[3];
     if (PSTEP) {
-        const int32_t syz = D.ny * D.nz;
-        const int i = l / syz;
-        const int r = l - i * syz;
-        const int j = r / D.nz;
-        const int k = r - j * D.nz;
-        dI[0] = (i == 0 ? (D.nx - 1) : -1) * syz; dI[1] = 0; dI[2] = (i + 1 == D.nx ? (1 - D.nx) : 1) * syz;
-        dJ[0] = (j == 0 ? (D.ny - 1) : -1) * D.nz; dJ[1] = 0; dJ[2] = (j + 1 == D.ny ? (1 - D.ny) : 1) * D.nz;
-        dK[0] = k == 0 ? (D.nz - 1) : -1; dK[1] = 0; dK[2] = k + 1 == D.nz ? (1 - D.nz) : 1;
+        const int32_t nx = D.nx, ny = D.ny, nz = D.nz, syz = ny * nz;
+        int32_t i, j, k, r;
+        if (D.n < (1 << 23)) {
+            i = split_div(l, syz, D.inv_syz, r);
+            j = split_div(r, nz, D.inv_nz, k);
+        } else {
+            i = l / syz; r = l - i * syz; j = r / nz; k = r - j * nz;
+        }
+        dI[0] = (i == 0 ? (nx - 1) : -1) * syz; dI[1] = 0; dI[2] = (i + 1 == nx ? (1 - nx) : 1) * syz;
+        dJ[0] = (j == 0 ? (ny - 1) : -1) * nz; dJ[1] = 0; dJ[2] = (j + 1 == ny ? (1 - ny) : 1) * nz;
+        dK[0] = k == 0 ? (nz - 1) : -1; dK[1] = 0; dK[2] = k + 1 == nz ? (1 - nz) : 1;
     }
     Unroll<0, Q>::run([&]<int q>() {
-        int64_t e;
+        const float *p;
         if (!PSTEP || q == 9) {
-            e = (int64_t)q * Np + n;
+            p = a.fq[q] + n;
         } else {
             const int32_t src = n + dI[1 - CX(q)] + dJ[1 - CY(q)] + dK[1 - CZ(q)];
-            e = (m & (1u << q)) ? ((int64_t)q * Np + n) : ((int64_t)OPP(q) * Np + src);
+            p = (m & (1u << q)) ? (a.fq[q] + n) : (a.fq[OPP(q)] + src);
         }
-        fv[q] = ST::template ld<q>(f + e);
+        fv[q] = ST::template ld<q>(p);
     });
     if (mv) {
         // Ladd's term on links to moving solids: 6 w_q rho_prev (c_q . U)
@@ -69,17 +83,17 @@ __global__ void __launch_bounds__(BLOCK, (BLOCK >= 256 ? 3 : BLOCK >= 128 ? 6 : 
     const C dd = PH::collide(fv, D.g[0], D.g[1], D.g[2], D.we, D.wo, ux, uy, uz);
     Unroll<0, Q>::run([&]<int q>() {
         if (!PSTEP) {
-            ST::template st<OPP(q)>(f + ((int64_t)OPP(q) * Np + n), fv[q]);
+            ST::template st<OPP(q)>(a.fq[OPP(q)] + n, fv[q]);
             return;
         }
-        int64_t e;
+        float *p;
         if (q == 9) {
-            e = 9 * Np + n;
+            p = a.fq[9] + n;
         } else {
             const int32_t dst = n + dI[1 + CX(q)] + dJ[1 + CY(q)] + dK[1 + CZ(q)];
-            e = (m & (1u << OPP(q))) ? ((int64_t)OPP(q) * Np + n) : ((int64_t)q * Np + dst);
+            p = (m & (1u << OPP(q))) ? (a.fq[OPP(q)] + n) : (a.fq[q] + dst);
         }
-        ST::template st<q>(f + e, fv[q]);
+        ST::template st<q>(p, fv[q]);
     });
     if (mv) a.dprev[n] = dd;
     if (a.write_moments) {

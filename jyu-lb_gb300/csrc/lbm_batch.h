@@ -21,11 +21,13 @@ struct BatchDomain {
     float we, wo;       // relaxation rates
     float g[3];         // body force
     float uw[3];        // velocity of the domain's moving solids
+    float inv_syz, inv_nz; // 1/(ny*nz), 1/nz for the site -> (i,j,k) split
 };
 
 struct BatchArgs {
     float *f;              // 19 * Np, f - w
     int64_t Np;            // slot stride (multiple of 128)
+    float *fq[19];         // f + q * Np: population rows, indexed by 32-bit site
     const BatchDomain *dom;
     const int32_t *tile_dom;
     const uint8_t *ncls;

@@ -1147,6 +1147,7 @@ BatchArgs batch_args(const jlb_batch *b, int write_moments) {
     BatchArgs a{};
     a.f = b->f;
     a.Np = b->Np;
+    for (int q = 0; q < 19; ++q) a.fq[q] = b->f + (size_t)q * b->Np;
     a.dom = b->d_dom;
     a.tile_dom = b->tile_dom;
     a.ncls = b->ncls;
@@ -1338,6 +1339,8 @@ int jlb_batch_create(int32_t scheme, const jlb_domain *doms, int32_t ndom, void 
         if (off + n >= 0x7fffff00LL) { b->err = "ensemble exceeds 2^31 sites"; return bail(JLB_ERR_UNSUPPORTED); }
         B.off = (int32_t)off;
         B.n = (int32_t)n;
+        B.inv_syz = 1.0f / (float)(B.ny * B.nz);
+        B.inv_nz = 1.0f / (float)B.nz;
         off += ((n + 127) / 128) * 128;
         const double tau_e = 0.5 + 3.0 * D.kvisc;
         const double we = 1.0 / tau_e;
