@@ -46,6 +46,16 @@ extern "C" {
 #define JLB_SOLID 0
 #define JLB_FLUID 1
 
+/* collision model of the time step */
+#define JLB_KERNEL_JYULB 0 /* the Python reference's (jyulb/D3Q19.pyx:655-940)  */
+#define JLB_KERNEL_CXX 1   /* the reference C++ executable's
+                              (include/kernel/kernel.cpp:410-550): FP64, BGK
+                              or TRT, periodic/wall faces, resting solids      */
+/* kernel_opts of JLB_KERNEL_CXX (its flow type and forcing switches,
+ * include/kernel/kernel.cpp:423-427) */
+#define JLB_CXX_LINEAR_EQ 1 /* linear ("Stokes flow") equilibrium            */
+#define JLB_CXX_FORCE2 2    /* second-order forcing ("external forcing")     */
+
 /* population storage / arithmetic of the time step */
 #define JLB_FP64 0 /* FP64 storage and arithmetic (parity path)          */
 #define JLB_FP32 1 /* FP32 storage of f_i - w_i, FP32 arithmetic          */
@@ -62,8 +72,15 @@ typedef struct jlb_config {
     int32_t precision;   /* JLB_FP64 / JLB_FP32 / JLB_FP16                   */
     double trt_magic;    /* TRT magic parameter; <= 0 selects the reference's
                             fixed 8(2-w)/(8-w) odd rate (magic 3/16)         */
+    int32_t kernel;      /* JLB_KERNEL_JYULB (0) or JLB_KERNEL_CXX           */
+    int32_t kernel_opts; /* JLB_CXX_* flags for JLB_KERNEL_CXX               */
     void *stream;        /* cudaStream_t to run on, or NULL                  */
 } jlb_config;
+/* With JLB_KERNEL_CXX, kvisc is the executable's dimensionless viscosity
+ * (tau = 0.5 + nu / c_s^2 with its c_s^2 = (1/sqrt 3)^2), g is its
+ * dimensionless gravity and the per-site acc field holds a dimensionless
+ * force density F_ext (the executable's F = F_ext + rho g) instead of an
+ * acceleration. */
 
 /* Argument validation of Solver.__cinit__ / _check_bc
  * (jyulb/isothermal.pyx:196-206, 378-426).  Writes the reference's message
@@ -95,6 +112,14 @@ int jlb_finalize_init(jlb_solver *s, uint8_t *phase, double *den, double *vel,
  * at the start of the call. */
 int jlb_evolve(jlb_solver *s, uint32_t tsteps, const double g[3], double *den,
                double *vel, const double *acc, uint32_t *tot);
+
+/* Uploads the per-site field of the halo-padded (NI,NJ,NK,3) array acc
+ * (acceleration, or force density with JLB_KERNEL_CXX) now, so that
+ * jlb_finalize_init uses it: the C++ executable's initial state includes the
+ * forcing term (include/kernel/kernel.cpp:339-345).  jlb_evolve with a
+ * non-NULL acc re-reads it as before; an all-zero or NULL acc switches the
+ * field off. */
+int jlb_set_acc(jlb_solver *s, const double *acc);
 
 /* Device-only stepping with the inputs of the last jlb_evolve call: no host
  * synchronisation, no host arrays.  write_moments != 0 stores den/vel of the

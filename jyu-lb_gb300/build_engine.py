@@ -31,6 +31,7 @@ UNITS = {
     "lbm_noalloc.cu": [],
     "lbm_batch.cu": [],
     "lbm_adjoint.cu": [],
+    "lbm_cxx.cu": ["-fmad=false"],
     # host arithmetic (relaxation rates, Ladd projections) must not be
     # FMA-contracted either: gcc contracts by default on aarch64
     "lbm_host.cpp": ["-x", "cu", "-Xcompiler", "-fopenmp", "-Xcompiler", "-ffp-contract=off"],

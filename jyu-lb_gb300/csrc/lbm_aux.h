@@ -25,6 +25,11 @@ int aux_download(int prec, const AuxGeom &g, const uint32_t *nmask, const void *
                  const void *uy, const void *uz, double *hden, double *hvel, cudaStream_t st);
 // interior of a device-accessible halo-padded (NI,NJ,NK,3) array -> SoA field
 int aux_acc_upload(int prec, const AuxGeom &g, const double *hacc, void *acc, cudaStream_t st);
+// initial state of the C++-executable model (lbm_cxx.cu); facc: SoA force
+// density field or NULL, gv: gravity, tau: relaxation time
+int aux_init_cxx(const AuxGeom &g, int scheme, int opts, const uint8_t *phase, const double *den,
+                 const double *vel, const double *facc, const double gv[3], double tau, double we, double wo,
+                 double *f, double *mden, double *mux, double *muy, double *muz, cudaStream_t st);
 int aux_reduce_blocks(int64_t N);
 // partial must hold 8 * nblocks doubles; out 8 doubles (device)
 int aux_reduce(int prec, const AuxGeom &g, const uint32_t *nmask, const void *den, const void *ux,

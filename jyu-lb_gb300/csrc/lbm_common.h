@@ -75,11 +75,17 @@ struct StepArgs {
                           // boundary nodes, [19][M] in the storage type
 };
 
+// options of the C++-executable collision model (lbm_cxx.cu)
+constexpr int CXX_LINEAR_EQ = 1; // linear ("Stokes") equilibrium instead of the quadratic one
+constexpr int CXX_FORCE2 = 2;    // second-order forcing term instead of the first-order one
+
 // launch entry points, one per precision translation unit
 // grid: `blocks` blocks of (a.bx, a.by) threads; returns a cudaError_t value
 int launch_step_fp64(const StepArgs &a, int scheme, bool pstep, bool accf, int blocks, cudaStream_t st);
 int launch_step_fp32(const StepArgs &a, int scheme, bool pstep, bool accf, int blocks, cudaStream_t st);
 int launch_step_fp16(const StepArgs &a, int scheme, bool pstep, bool accf, int blocks, cudaStream_t st);
+// the C++-executable collision model (lbm_cxx.cu), FP64; opts: CXX_* flags
+int launch_step_cxx(const StepArgs &a, int scheme, int opts, bool pstep, bool accf, int blocks, cudaStream_t st);
 // bulk-copy staged variants (lbm_step_tma.cuh): persistent grid over
 // `ntiles` row tiles of 128 sites, then `nsb` boundary-node blocks; a
 // timed-out mbarrier wait sets *err

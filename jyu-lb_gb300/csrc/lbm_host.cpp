@@ -58,6 +58,7 @@ struct jlb_solver {
     int prec = 0;
     size_t ssz = 8, csz = 8;  // storage / compute element sizes
     double we = 0, wo = 0;
+    double tau = 0;       // relaxation time of the C++-executable model
     AuxGeom geom{};
     cudaStream_t st = nullptr;
     bool own_stream = false;
@@ -585,6 +586,8 @@ int launch_one(jlb_solver *s, const StepArgs &a, bool pstep) {
             r = launch_step_tma_fp32(a, s->cfg.rlx_scheme, pstep, s->accf, s->tma_grid, ntiles, nsb, s->d_err, s->st);
         else
             r = launch_step_tma_fp16(a, s->cfg.rlx_scheme, pstep, s->accf, s->tma_grid, ntiles, nsb, s->d_err, s->st);
+    } else if (s->cfg.kernel == JLB_KERNEL_CXX) {
+        r = launch_step_cxx(a, s->cfg.rlx_scheme, s->cfg.kernel_opts, pstep, s->accf, blocks, s->st);
     } else if (s->prec == PREC_FP64) r = launch_step_fp64(a, s->cfg.rlx_scheme, pstep, s->accf, blocks, s->st);
     else if (s->prec == PREC_FP32) r = launch_step_fp32(a, s->cfg.rlx_scheme, pstep, s->accf, blocks, s->st);
     else r = launch_step_fp16(a, s->cfg.rlx_scheme, pstep, s->accf, blocks, s->st);
@@ -753,6 +756,18 @@ int jlb_check_config(const jlb_config *cfg, char *msg, size_t msg_len) {
     if (std::isnan(cfg->trt_magic)) return bad("Invalid TRT magic parameter input.");
     for (int d = 0; d < 3; ++d)
         if (!std::isfinite(cfg->g[d])) return bad("Invalid gravity input.");
+    if (cfg->kernel != JLB_KERNEL_JYULB && cfg->kernel != JLB_KERNEL_CXX) return bad("Invalid collision kernel input.");
+    if (cfg->kernel == JLB_KERNEL_CXX) {
+        if (cfg->rlx_scheme == JLB_REGULARIZATION)
+            return bad("The C++-executable kernel supports the BGK and TRT schemes.");
+        if (cfg->precision != JLB_FP64) return bad("The C++-executable kernel runs in FP64.");
+        for (int f = 0; f < 6; ++f)
+            if (bc[f] != JLB_PERIODIC && bc[f] != JLB_WALL)
+                return bad("The C++-executable kernel supports periodic and wall faces.");
+        if (cfg->kernel_opts & ~(JLB_CXX_LINEAR_EQ | JLB_CXX_FORCE2)) return bad("Invalid kernel options input.");
+    } else if (cfg->kernel_opts != 0) {
+        return bad("Invalid kernel options input.");
+    }
     return JLB_OK;
 }
 
@@ -778,12 +793,21 @@ int jlb_create(const jlb_config *cfg, jlb_solver **out) {
     s->ssz = s->prec == PREC_FP64 ? 8 : s->prec == PREC_FP32 ? 4 : 2;
     s->csz = s->prec == PREC_FP64 ? 8 : 4;
     for (int d = 0; d < 3; ++d) s->g[d] = cfg->g[d];
-    // relaxation rates (jyulb/isothermal.pyx:274-287)
-    const double tau_e = 0.5 + 3.0 * cfg->kvisc;
-    s->we = 1.0 / tau_e;
-    if (cfg->rlx_scheme == JLB_TRT) {
-        if (cfg->trt_magic > 0.0) s->wo = 1.0 / (cfg->trt_magic / (tau_e - 0.5) + 0.5);
-        else s->wo = 8.0 * (2.0 - s->we) / (8.0 - s->we);
+    if (cfg->kernel == JLB_KERNEL_CXX) {
+        // the executable's rates (include/collision/collision.cpp:14-24,
+        // :64-76) with its c_s^2 = (1/sqrt 3)^2
+        const double ct = 1.0 / std::sqrt(3.0), ct2 = ct * ct, inv_ct2 = 1.0 / ct2;
+        s->tau = 0.5 + inv_ct2 * cfg->kvisc;
+        s->we = 1.0 / s->tau;
+        s->wo = cfg->rlx_scheme == JLB_TRT ? 8.0 * ((2.0 - s->we) / (8.0 - s->we)) : s->we;
+    } else {
+        // relaxation rates (jyulb/isothermal.pyx:274-287)
+        const double tau_e = 0.5 + 3.0 * cfg->kvisc;
+        s->we = 1.0 / tau_e;
+        if (cfg->rlx_scheme == JLB_TRT) {
+            if (cfg->trt_magic > 0.0) s->wo = 1.0 / (cfg->trt_magic / (tau_e - 0.5) + 0.5);
+            else s->wo = 8.0 * (2.0 - s->we) / (8.0 - s->we);
+        }
     }
     s->geom = AuxGeom{s->nx, s->ny, s->nz, s->NI, s->NJ, s->NK, s->N, s->Np};
     int r = JLB_OK;
@@ -878,8 +902,14 @@ int jlb_finalize_init(jlb_solver *s, uint8_t *phase, double *den, double *vel, u
         CK(cudaMemcpyAsync(dvel, vel, 3 * nb * sizeof(double), cudaMemcpyHostToDevice, s->st));
         CK(cudaMemsetAsync(s->f, 0, (size_t)19 * s->Np * s->ssz, s->st));
         for (int c = 0; c < 4; ++c) CK(cudaMemsetAsync(s->mom[c], 0, (size_t)s->Np * s->csz, s->st));
-        r = aux_init(s->prec, s->geom, dph, dden, dvel, s->we, s->f, s->mom[0], s->mom[1], s->mom[2], s->mom[3],
-                     s->st);
+        if (s->cfg.kernel == JLB_KERNEL_CXX)
+            r = aux_init_cxx(s->geom, s->cfg.rlx_scheme, s->cfg.kernel_opts, dph, dden, dvel,
+                             s->accf ? (const double *)s->acc : nullptr, s->g, s->tau, s->we, s->wo, (double *)s->f,
+                             (double *)s->mom[0], (double *)s->mom[1], (double *)s->mom[2], (double *)s->mom[3],
+                             s->st);
+        else
+            r = aux_init(s->prec, s->geom, dph, dden, dvel, s->we, s->f, s->mom[0], s->mom[1], s->mom[2],
+                         s->mom[3], s->st);
         ++s->launches;
         cudaError_t es = cudaStreamSynchronize(s->st);
         cudaFree(dph); cudaFree(dden); cudaFree(dvel);
@@ -892,6 +922,47 @@ int jlb_finalize_init(jlb_solver *s, uint8_t *phase, double *den, double *vel, u
     s->parity = 0;
     s->init_done = true;
     if (nfluid) *nfluid = cnt;
+    return JLB_OK;
+}
+
+// per-site field from a halo-padded (NI,NJ,NK,3) host array; an all-zero or
+// NULL array switches the field off
+static int set_acc_field(jlb_solver *s, const double *acc) {
+    bool accf = false;
+    if (acc) {
+        for (int I = 1; I < s->NI - 1 && !accf; ++I)
+            for (int J = 1; J < s->NJ - 1 && !accf; ++J)
+                for (int K = 1; K < s->NK - 1; ++K) {
+                    const double *a = acc + 3 * fidx(s, I, J, K);
+                    if (a[0] != 0.0 || a[1] != 0.0 || a[2] != 0.0) { accf = true; break; }
+                }
+    }
+    if (accf) {
+        if (!s->acc) CK(cudaMalloc(&s->acc, (size_t)3 * s->Np * s->csz));
+        const double *da = (const double *)dev_view(acc);
+        if (da) {
+            CKR(aux_acc_upload(s->prec, s->geom, da, s->acc, s->st));
+            s->h2d_bytes += (uint64_t)s->N * 3 * sizeof(double);
+        } else {
+            double *tmp = nullptr;
+            CK(cudaMalloc(&tmp, (size_t)3 * s->NCNT * sizeof(double)));
+            cudaMemcpyAsync(tmp, acc, (size_t)3 * s->NCNT * sizeof(double), cudaMemcpyHostToDevice, s->st);
+            int rr = aux_acc_upload(s->prec, s->geom, tmp, s->acc, s->st);
+            cudaStreamSynchronize(s->st);
+            cudaFree(tmp);
+            CKR(rr);
+        }
+        ++s->launches;
+    }
+    if (accf != s->accf) { s->accf = accf; ++s->args_version; }
+    return JLB_OK;
+}
+
+int jlb_set_acc(jlb_solver *s, const double *acc) {
+    if (!s) return fail(s, JLB_ERR_INVALID_ARG, "NULL solver");
+    int r = set_acc_field(s, acc);
+    if (r) return r;
+    CK(cudaStreamSynchronize(s->st));
     return JLB_OK;
 }
 
@@ -936,35 +1007,11 @@ int jlb_evolve(jlb_solver *s, uint32_t tsteps, const double g[3], double *den, d
     t1 = clk::now();
     if (r) return r;
     // acceleration field (read every step by the reference, jyulb/isothermal.pyx:1293-1295)
-    bool accf = false;
-    if (acc) {
-        for (int I = 1; I < s->NI - 1 && !accf; ++I)
-            for (int J = 1; J < s->NJ - 1 && !accf; ++J)
-                for (int K = 1; K < s->NK - 1; ++K) {
-                    const double *a = acc + 3 * fidx(s, I, J, K);
-                    if (a[0] != 0.0 || a[1] != 0.0 || a[2] != 0.0) { accf = true; break; }
-                }
-    }
-    if (accf) {
-        if (!s->acc) CK(cudaMalloc(&s->acc, (size_t)3 * s->Np * s->csz));
-        const double *da = (const double *)dev_view(acc);
-        if (da) {
-            CKR(aux_acc_upload(s->prec, s->geom, da, s->acc, s->st));
-            s->h2d_bytes += (uint64_t)s->N * 3 * sizeof(double);
-        } else {
-            double *tmp = nullptr;
-            CK(cudaMalloc(&tmp, (size_t)3 * s->NCNT * sizeof(double)));
-            cudaMemcpyAsync(tmp, acc, (size_t)3 * s->NCNT * sizeof(double), cudaMemcpyHostToDevice, s->st);
-            int rr = aux_acc_upload(s->prec, s->geom, tmp, s->acc, s->st);
-            cudaStreamSynchronize(s->st);
-            cudaFree(tmp);
-            CKR(rr);
-        }
-        ++s->launches;
-    }
-    if (accf != s->accf) { s->accf = accf; ++s->args_version; }
+    if ((r = set_acc_field(s, acc))) return r;
     s->host_t[2] += since(t1);
     t1 = clk::now();
+    if (s->cfg.kernel == JLB_KERNEL_CXX && s->M > 0)
+        return fail(s, JLB_ERR_UNSUPPORTED, "the C++-executable kernel has no moving solids");
     r = run_steps(s, tsteps, true);
     if (r) return r;
     s->host_t[3] += since(t1);
@@ -983,6 +1030,8 @@ int jlb_step(jlb_solver *s, uint32_t tsteps, int write_moments) {
     if (!s) return fail(s, JLB_ERR_INVALID_ARG, "NULL solver");
     if (!s->init_done) return fail(s, JLB_ERR_STATE, "finalize_init has not been called");
     if (s->nfluid < 1) return JLB_OK;
+    if (s->cfg.kernel == JLB_KERNEL_CXX && s->M > 0)
+        return fail(s, JLB_ERR_UNSUPPORTED, "the C++-executable kernel has no moving solids");
     int r = run_steps(s, tsteps, write_moments != 0);
     if (r) return r;
     s->tot += tsteps;
@@ -1621,6 +1670,8 @@ int jlb_adj_create(const jlb_config *cfg, const uint8_t *phase, int32_t loss_pla
     if (cfg->rlx_scheme == JLB_REGULARIZATION)
         return afail(nullptr, JLB_ERR_UNSUPPORTED, "adjoint supports BGK and TRT");
     if (checkpoint_every < 1) return afail(nullptr, JLB_ERR_INVALID_ARG, "checkpoint interval must be >= 1");
+    if (cfg->kernel != JLB_KERNEL_JYULB)
+        return afail(nullptr, JLB_ERR_UNSUPPORTED, "adjoint supports the jyulb collision kernel");
     for (int f = 1; f < 6; ++f)
         if (cfg->bc[f] == JLB_FIXED_VEL)
             return afail(nullptr, JLB_ERR_UNSUPPORTED, "adjoint: FIXED_VEL is supported on face 1X only");

@@ -14,6 +14,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <cuda_fp16.h>
+#include <type_traits>
 #include "lbm_common.h"
 
 namespace jlb {
@@ -88,6 +89,16 @@ struct StoreF16 {
     template <int q> __device__ static void st(S *p, C v) { *p = __float2half_rn(v * enc<q>()); }
 };
 
+// physics policies whose forcing takes a force density F = F_field + rho g
+// (the C++ executable's model) declare force_density = true; the others
+// take an acceleration a = g + a_field
+template <class PH, class = void> struct uses_force_density {
+    static constexpr bool value = false;
+};
+template <class PH> struct uses_force_density<PH, std::void_t<decltype(PH::force_density)>> {
+    static constexpr bool value = PH::force_density;
+};
+
 // compile-time loop
 template <int I, int N> struct Unroll {
     template <class F> __device__ __forceinline__ static void run(F &&f) {
@@ -155,17 +166,26 @@ __device__ __forceinline__ void dense_node(const StepArgs &a, int b) {
         fv[q] = ST::template ld<q>(f + e);
     });
 
-    C ax, ay, az;
-    if (ACCF) {
-        const C *acc = (const C *)a.acc;
-        ax = (C)a.g[0] + __ldg(acc + n);
-        ay = (C)a.g[1] + __ldg(acc + Np + n);
-        az = (C)a.g[2] + __ldg(acc + 2 * Np + n);
+    C ux, uy, uz, rho;
+    if constexpr (uses_force_density<PH>::value) {
+        C fx = 0, fy = 0, fz = 0;
+        if (ACCF) {
+            const C *acc = (const C *)a.acc;
+            fx = __ldg(acc + n); fy = __ldg(acc + Np + n); fz = __ldg(acc + 2 * Np + n);
+        }
+        rho = PH::collide_fd(fv, (C)a.g[0], (C)a.g[1], (C)a.g[2], fx, fy, fz, (C)a.w_e, (C)a.w_o, ux, uy, uz);
     } else {
-        ax = (C)a.g[0]; ay = (C)a.g[1]; az = (C)a.g[2];
+        C ax, ay, az;
+        if (ACCF) {
+            const C *acc = (const C *)a.acc;
+            ax = (C)a.g[0] + __ldg(acc + n);
+            ay = (C)a.g[1] + __ldg(acc + Np + n);
+            az = (C)a.g[2] + __ldg(acc + 2 * Np + n);
+        } else {
+            ax = (C)a.g[0]; ay = (C)a.g[1]; az = (C)a.g[2];
+        }
+        rho = PH::collide(fv, ax, ay, az, (C)a.w_e, (C)a.w_o, ux, uy, uz);
     }
-    C ux, uy, uz;
-    const C rho = PH::collide(fv, ax, ay, az, (C)a.w_e, (C)a.w_o, ux, uy, uz);
 
     // scatter: a population heading into a solid is stored back into this
     // node's opposite slot
@@ -240,17 +260,26 @@ __device__ __forceinline__ void special_node(const StepArgs &a, int b) {
         Unroll<0, Q>::run([&]<int q>() { ST::template st<q>(tee + ((int64_t)q * M + t), fv[q]); });
     }
 
-    C ax, ay, az;
-    if (ACCF) {
-        const C *acc = (const C *)a.acc;
-        ax = (C)a.g[0] + __ldg(acc + n);
-        ay = (C)a.g[1] + __ldg(acc + Np + n);
-        az = (C)a.g[2] + __ldg(acc + 2 * Np + n);
+    C ux, uy, uz, rho;
+    if constexpr (uses_force_density<PH>::value) {
+        C fx = 0, fy = 0, fz = 0;
+        if (ACCF) {
+            const C *acc = (const C *)a.acc;
+            fx = __ldg(acc + n); fy = __ldg(acc + Np + n); fz = __ldg(acc + 2 * Np + n);
+        }
+        rho = PH::collide_fd(fv, (C)a.g[0], (C)a.g[1], (C)a.g[2], fx, fy, fz, (C)a.w_e, (C)a.w_o, ux, uy, uz);
     } else {
-        ax = (C)a.g[0]; ay = (C)a.g[1]; az = (C)a.g[2];
+        C ax, ay, az;
+        if (ACCF) {
+            const C *acc = (const C *)a.acc;
+            ax = (C)a.g[0] + __ldg(acc + n);
+            ay = (C)a.g[1] + __ldg(acc + Np + n);
+            az = (C)a.g[2] + __ldg(acc + 2 * Np + n);
+        } else {
+            ax = (C)a.g[0]; ay = (C)a.g[1]; az = (C)a.g[2];
+        }
+        rho = PH::collide(fv, ax, ay, az, (C)a.w_e, (C)a.w_o, ux, uy, uz);
     }
-    C ux, uy, uz;
-    const C rho = PH::collide(fv, ax, ay, az, (C)a.w_e, (C)a.w_o, ux, uy, uz);
 
     S *fo = a.fout ? (S *)a.fout : f;
     Unroll<0, Q>::run([&]<int q>() {

@@ -25,11 +25,12 @@ units convert as the executable's kernel does (include/kernel/kernel.cpp:
 410-465): c_r = dr/dt, density / ref_den, velocity / c_r, viscosity
 dt/dr^2, gravity dt^2/dr, force density / (ref_den c_r / dt).
 
-The collision is the Python reference's (jyulb/D3Q19.pyx:655-940): BGK, TRT
-(magic 3/16, as in both references) and regularized.  MRT falls back to TRT
-with the executable's warning.  The executable's linear (Stokes) equilibrium
-and first-order forcing are not available: flow type 0 runs the quadratic
-equilibrium with a warning.
+By default the run uses the executable's own collision model on the GPU
+(``physics="cxx"``: linear equilibrium for Stokes flow, quadratic otherwise;
+first-order forcing, second-order with external forcing; BGK or TRT, other
+operators fall back to TRT with the executable's warning) and reproduces its
+output files.  ``physics="jyulb"`` runs this package's reference collision
+(BGK, TRT, regularized) instead and admits the Zou-He faces of the face lines.
 """
 from __future__ import annotations
 
@@ -100,8 +101,12 @@ def _warn(msg, default):
     print(f"Warning: {msg}!Warning: using default {default}!")
 
 
-def parse_input_script(text, face_lines=True):
-    """InputScript from the text of an input script."""
+def parse_input_script(text, face_lines=None):
+    """InputScript from the text of an input script.  face_lines: True for
+    the layout with six face lines (tube.in), False for the executable
+    parser's layout without them, None to tell them apart by the number of
+    value lines after the collision operator (nine or eight with face lines,
+    three or two without)."""
     p = InputScript()
     rd = _Lines(text)
     line = rd.next_line()
@@ -142,6 +147,9 @@ def parse_input_script(text, face_lines=True):
         _warn("invalid collision operator argument", "collision operator")
     else:
         p.collision_operator = co
+    if face_lines is None:
+        rest = [l for l in rd.lines[rd.pos:] if not l.startswith("#")]
+        face_lines = len(rest) >= 8
     if face_lines:
         faces = []
         for f in range(6):
@@ -178,7 +186,7 @@ def evol_row(step_col, time_col, info):
 def scaled_info(solver, p):
     """Flow information of the solver (lattice units) in the script's
     physical units."""
-    cr = p.dr / p.dt
+    cr = units(p)["cr"]
     fi = solver.flow_info(1.0)
     out = dict(fi)
     for k in ("tot_den", "max_den", "min_den"):
@@ -190,46 +198,69 @@ def scaled_info(solver, p):
     return out
 
 
-def build_solver(p, precision=0, stream=None):
-    """A jyulb Solver set up from the script and its raw input files."""
+def units(p):
+    """The executable's unit conversions in its own evaluation order
+    (include/kernel/kernel.cpp:414-419, 457-465): lattice speed c_r = dr/dt,
+    body-force unit ref_den c_r / dt, viscosity / (dr c_r), gravity dt / c_r."""
+    inv_dt = 1.0 / p.dt
+    cr = p.dr * inv_dt
+    inv_cr = 1.0 / cr
+    bf_unit = p.ref_den * inv_dt * cr
+    return dict(cr=cr, inv_cr=inv_cr, inv_dr=1.0 / p.dr, inv_ref_den=1.0 / p.ref_den, inv_bf_unit=1.0 / bf_unit,
+                kvisc=(1.0 / p.dr) * inv_cr * p.kvisc, g=[p.dt * inv_cr * gv for gv in p.g])
+
+
+def build_solver(p, precision=0, stream=None, physics="cxx"):
+    """A jyulb Solver set up from the script and its raw input files.
+
+    physics="cxx" runs the executable's own collision model (linear or
+    quadratic equilibrium from the flow type, first- or second-order forcing
+    from the external-forcing switch; periodic and wall faces only) and
+    reproduces its output; physics="jyulb" runs this package's reference
+    collision and also accepts Zou-He faces."""
     from .isothermal import Solver
 
-    cr = p.dr / p.dt
-    kvisc = p.kvisc * p.dt / (p.dr * p.dr)
-    g = np.array(p.g, dtype=np.float64) * (p.dt * p.dt / p.dr)
-    scheme = {CPP_BGK: BGK, CPP_TRT: TRT, CPP_REG: REGULARIZATION}.get(p.collision_operator)
+    u = units(p)
+    inv_cr = u["inv_cr"]
+    if physics == "cxx":
+        scheme = {CPP_BGK: BGK, CPP_TRT: TRT}.get(p.collision_operator)
+    else:
+        scheme = {CPP_BGK: BGK, CPP_TRT: TRT, CPP_REG: REGULARIZATION}.get(p.collision_operator)
+        if p.flow_type == STOKES_FLOW:
+            print("Warning: the linear (Stokes) equilibrium needs physics='cxx'; using the quadratic equilibrium")
     if scheme is None:
         print("Warning: using default collision operator (TRT)")
         scheme = TRT
-    if p.flow_type == STOKES_FLOW:
-        print("Warning: the linear (Stokes) equilibrium is not available; using the quadratic equilibrium")
     bc = []
     for code, _ in p.faces:
         if code == FACE_SHEAR:
             raise ValueError("shear-wall faces are not supported")
+        if physics == "cxx" and code not in (FACE_PERIODIC, FACE_WALL):
+            raise ValueError("the executable's collision model has no Zou-He faces; use physics='jyulb'")
         bc.append({FACE_PERIODIC: PERIODIC, FACE_WALL: WALL, FACE_DEN: FIXED_DEN, FACE_VEL: FIXED_VEL}[code])
     geom = raw_io.read_geom(p.base, p.size)
     if geom is None:
         raise FileNotFoundError(f"{p.base}.geom.in.raw")
     phase = raw_io.geom_to_phase(geom)
     fluid = phase != 0
-    s = Solver(np.array(p.size, dtype=np.int32), scheme, kvisc, g, np.array(bc, dtype=np.int32),
-               precision=precision, stream=stream)
+    kw = {}
+    if physics == "cxx":
+        kw = dict(kernel="cxx", stokes=p.flow_type == STOKES_FLOW, second_order_forcing=bool(p.external_forcing))
+    s = Solver(np.array(p.size, dtype=np.int32), scheme, u["kvisc"], np.array(u["g"], dtype=np.float64),
+               np.array(bc, dtype=np.int32), precision=precision, stream=stream, **kw)
     s.get_phase()[:] = phase
-    den = np.ones(tuple(p.size))
-    vel = np.zeros(tuple(p.size) + (3,))
+    # dimensional fields with the executable's defaults, then scaled by the
+    # same multiplications (kernel.cpp:335-337)
     den_in = np.full(tuple(p.size), p.ref_den)
-    if raw_io.read_den(p.base, fluid, den_in):
-        den = den_in / p.ref_den
-    else:
+    if not raw_io.read_den(p.base, fluid, den_in):
         print("No input file for density: using default initial density.")
         print("--------------------------------------------------------------")
     vel_in = np.zeros(tuple(p.size) + (3,))
-    if raw_io.read_vel(p.base, fluid, vel_in):
-        vel = vel_in / cr
-    else:
+    if not raw_io.read_vel(p.base, fluid, vel_in):
         print("No input file for velocity: using default initial velocity.")
         print("--------------------------------------------------------------")
+    den = den_in * u["inv_ref_den"]
+    vel = vel_in * inv_cr
     # Zou-He face data sit on the face layers of den / vel
     for f, (code, data) in enumerate(p.faces):
         ax, hi = f // 2, f % 2
@@ -237,31 +268,34 @@ def build_solver(p, precision=0, stream=None):
         sl[ax] = -1 if hi else 0
         sl = tuple(sl)
         if code == FACE_DEN:
-            den[sl] = data[0] / p.ref_den
+            den[sl] = data[0] * u["inv_ref_den"]
             t = [a for a in range(3) if a != ax]
-            vel[sl + (t[0],)] = data[1] / cr
-            vel[sl + (t[1],)] = data[2] / cr
+            vel[sl + (t[0],)] = data[1] * inv_cr
+            vel[sl + (t[1],)] = data[2] * inv_cr
             vel[sl + (ax,)] = 0.0
         elif code == FACE_VEL:
             for a in range(3):
-                vel[sl + (a,)] = data[a] / cr
+                vel[sl + (a,)] = data[a] * inv_cr
     s.get_den()[:] = den
     s.get_vel()[:] = vel
     if p.external_forcing:
         frc = np.zeros(tuple(p.size) + (3,))
         if raw_io.read_frc(p.base, fluid, frc):
-            # force density -> per-site acceleration with the initial density
-            bf_unit = p.ref_den * cr / p.dt
             acc = s.get_acc()
             acc[:] = 0.0
-            acc[fluid] = (frc[fluid] / bf_unit) / den[fluid][:, None]
+            if physics == "cxx":
+                acc[fluid] = frc[fluid] * u["inv_bf_unit"]  # force density, as the executable uses it
+            else:
+                # force density -> per-site acceleration with the initial density
+                acc[fluid] = (frc[fluid] * u["inv_bf_unit"]) / den[fluid][:, None]
     return s, fluid
 
 
-def run(p, precision=0, out=sys.stdout):
+def run(p, precision=0, out=None, physics="cxx"):
     """The executable's main loop on the GPU; returns the solver."""
-    s, fluid = build_solver(p, precision)
-    cr = p.dr / p.dt
+    out = sys.stdout if out is None else out
+    s, fluid = build_solver(p, precision, physics=physics)
+    cr = units(p)["cr"]
     nf = s.finalize_init()
     evol = open(p.base + ".evol", "w")
     evol.write(EVOL_HEADER + "\n")
@@ -288,13 +322,21 @@ def run(p, precision=0, out=sys.stdout):
     print("==============================================================", file=out)
     den = np.array(s.get_den()) * p.ref_den
     vel = np.array(s.get_vel()) * cr
-    raw_io.write_den(p.base, den, fluid, p.ref_den)
+    # solid sites: the executable writes its node data's initial density,
+    # a member its constructor never sets (include/common/data.h:75-87); it
+    # reads 0 in practice, and 0 is written here
+    raw_io.write_den(p.base, den, fluid, 0.0)
     raw_io.write_vel(p.base, vel, fluid)
     return s
 
 
 def main(argv=None):
     argv = sys.argv[1:] if argv is None else argv
+    physics = "cxx"
+    if "--physics" in argv:
+        i = argv.index("--physics")
+        physics = argv[i + 1]
+        argv = argv[:i] + argv[i + 2:]
     if not argv:
         print("Warning: not enough input arguments!")
         print("Warning: using default simulation parameters!")
@@ -306,7 +348,7 @@ def main(argv=None):
             print("Warning: unable to open input script!Warning: using default simulation parameters!")
             text = None
         p = parse_input_script(text) if text is not None else InputScript()
-    run(p)
+    run(p, physics=physics)
     return 0
 
 

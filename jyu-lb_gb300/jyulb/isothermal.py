@@ -83,7 +83,8 @@ class Solver:
     """D3Q19 isothermal lattice-Boltzmann solver (see the module docstring)."""
 
     def __init__(self, lat_size, rlx_scheme=BGK, kvisc=1.0 / 6.0, g=None, bc=None, *,
-                 precision=FP64, trt_magic=None, stream=None):
+                 precision=FP64, trt_magic=None, stream=None, kernel='jyulb', stokes=False,
+                 second_order_forcing=False):
         self.error_msg = ''
         lat = [int(v) for v in np.asarray(lat_size).reshape(-1)[:3]]
         # argument checks of jyulb/isothermal.pyx:196-230
@@ -115,6 +116,20 @@ class Solver:
         self.rlx_scheme = int(rlx_scheme)
         self.precision = int(precision)
         self.trt_magic = None if trt_magic is None else float(trt_magic)
+        # collision model: 'jyulb' (this package's reference) or 'cxx' (the
+        # reference C++ executable's, include/kernel/kernel.cpp:410-550, with
+        # its linear "Stokes" equilibrium and second-order forcing switches;
+        # kvisc and g are then its dimensionless values and acc holds a
+        # force density)
+        if kernel not in ('jyulb', 'cxx'):
+            raise ValueError('Invalid collision kernel input.')
+        self.kernel = kernel
+        self.kernel_opts = 0
+        if kernel == 'cxx':
+            self.kernel_opts = ((_native.JLB_CXX_LINEAR_EQ if stokes else 0) |
+                                (_native.JLB_CXX_FORCE2 if second_order_forcing else 0))
+        elif stokes or second_order_forcing:
+            raise ValueError('Invalid kernel options input.')
         self._stream = stream
         self.tot_tsteps = 0
         self.init_done = 0
@@ -156,6 +171,8 @@ class Solver:
         cfg.bc[:] = self._bc
         cfg.precision = self.precision
         cfg.trt_magic = 0.0 if self.trt_magic is None else self.trt_magic
+        cfg.kernel = _native.JLB_KERNEL_CXX if self.kernel == 'cxx' else _native.JLB_KERNEL_JYULB
+        cfg.kernel_opts = self.kernel_opts
         cfg.stream = None if self._stream is None else int(self._stream)
         h = ctypes.c_void_p()
         rc = lib.jlb_create(ctypes.byref(cfg), ctypes.byref(h))
@@ -231,6 +248,11 @@ class Solver:
         (jyulb/isothermal.pyx:1333-1365)."""
         if self.error_occured():
             raise RuntimeError('Invalid solver setup: finalization aborted!')
+        if self._acc_exposed and self.kernel == 'cxx':
+            # the C++ executable's initial state includes the forcing term
+            rc = self._lib.jlb_set_acc(self._h, _native.dptr(self._acc))
+            if rc != _native.JLB_OK:
+                self._raise(rc)
         n = ctypes.c_uint64()
         rc = self._lib.jlb_finalize_init(self._h, _native.u8ptr(self.phase), _native.dptr(self.den),
                                          _native.dptr(self.vel), ctypes.byref(n))

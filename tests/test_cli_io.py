@@ -120,13 +120,13 @@ def test_cli_run_matches_solver(tmp_path, capsys):
     geom = np.where((X - 2.5) ** 2 + (Y - 2.0) ** 2 <= 4.0, 255, 0).astype(np.uint8)[:, :, None].repeat(nz, 2)
     raw_io.write_geom(p.base, geom)
     os.rename(p.base + ".geom.out.raw", p.base + ".geom.in.raw")
-    s = cli.run(p)
+    s = cli.run(p, physics="jyulb")
     out = capsys.readouterr().out
     assert "tstep 40, tot.mass" in out and "MFLUPS" in out
     rows = [l.split("\t") for l in open(p.base + ".evol").read().splitlines()[1:]]
     assert [r[0] for r in rows] == ["0", "3", "7", "10"]  # dt * step with dt = 0.25
     # the same run through the Solver API
-    ref, fluid = cli.build_solver(p)
+    ref, fluid = cli.build_solver(p, physics="jyulb")
     ref.finalize_init()
     for n in (15, 15, 10):
         ref.evolve(n)
