@@ -14,7 +14,8 @@ Our arm (default) prints one JSON line with
   roofline     HBM roofline of the step kernel: 152 algorithmic bytes per fluid
                site (19 FP32 loads + 19 FP32 stores) per launch / launch time;
   fp64         the same for the FP64 plain path (304 B per site);
-  error        relative L2 velocity error of FP32 against FP64 after
+  fp16         the same for FP16 storage with FP32 arithmetic (76 B per site);
+  error        relative L2 velocity errors of FP32 and FP16 against FP64 after
                --err-steps steps of the same cavity;
   cpu_baseline the reference's own OpenMP solver on this host's cores.
 `--impl reference` times only the reference's CPU solver on the same config.
@@ -66,9 +67,12 @@ class ClockSampler:
               "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
               "clocks_event_reasons.sw_power_cap")
 
+    _count = 0
+
     def __init__(self, index=0):
         self.proc = None
-        self.out = os.path.join("/tmp", f"jlb_clocks_{os.getpid()}.csv")
+        ClockSampler._count += 1
+        self.out = os.path.join("/tmp", f"jlb_clocks_{os.getpid()}_{ClockSampler._count}.csv")
         self.index = index
 
     def __enter__(self):
@@ -162,17 +166,22 @@ def time_e2e(s, nf, steps, warmup):
 
 
 def l2_error(n, steps, stream):
-    from jyulb.defs import FP32, FP64
+    """Relative L2 velocity errors of FP32 and FP16 storage against FP64
+    after `steps` steps of the cavity."""
+    from jyulb.defs import FP16, FP32, FP64
 
     s64, nf = cavity(n, FP64, stream)
     s64.evolve(steps)
     v64 = np.array(s64.get_vel())
     del s64
-    s32, _ = cavity(n, FP32, stream)
-    s32.evolve(steps)
-    v32 = np.array(s32.get_vel())
-    del s32
-    return float(np.linalg.norm(v32 - v64) / np.linalg.norm(v64))
+    errs = []
+    for prec in (FP32, FP16):
+        s, _ = cavity(n, prec, stream)
+        s.evolve(steps)
+        v = np.array(s.get_vel())
+        del s
+        errs.append(float(np.linalg.norm(v - v64) / np.linalg.norm(v64)))
+    return errs
 
 
 def reference_mlups(n, steps, warmup, threads=None, budget_s=20.0):
@@ -642,7 +651,7 @@ def main():
         import torch.distributed as dist
 
         dist.init_process_group("nccl")
-    from jyulb.defs import FP32, FP64
+    from jyulb.defs import FP16, FP32, FP64
 
     n = args.size
     tstream = torch.cuda.Stream()
@@ -671,7 +680,12 @@ def main():
         mlups64, ms64, _ = time_device(s64, nf, max(args.steps // 4, 20), args.warmup, torch, tstream)
     del s64
     torch.cuda.empty_cache()
-    err = l2_error(n, args.err_steps, stream) if args.err_steps > 0 else None
+    s16, _ = cavity(n, FP16, stream)
+    with ClockSampler(local) as clk16:
+        mlups16, ms16, _ = time_device(s16, nf, args.steps, args.warmup, torch, tstream)
+    del s16
+    torch.cuda.empty_cache()
+    err, err16 = l2_error(n, args.err_steps, stream) if args.err_steps > 0 else (None, None)
     peak, peak_kind = measured_peak()
     ach = nf * BYTES_FP32 / (ms_launch * 1e-3) / 1e9
     ach64 = nf * BYTES_FP64 / (ms64 * 1e-3) / 1e9
@@ -699,7 +713,11 @@ def main():
                  "roofline_frac": round(ach64 / peak, 4), "achieved_gbs": round(ach64, 1),
                  "bytes_per_site": BYTES_FP64, "fp32_over_fp64": round(mlups / mlups64, 3),
                  "clocks": clk64.summary()},
-        "error": {"vel_rel_l2_fp32_vs_fp64": err, "steps": args.err_steps},
+        "fp16": {"value": round(mlups16, 3), "unit": "MLUPS", "ms_per_step": round(ms16, 5),
+                 "roofline_frac": round(nf * 76 / (ms16 * 1e-3) / 1e9 / peak, 4),
+                 "achieved_gbs": round(nf * 76 / (ms16 * 1e-3) / 1e9, 1), "bytes_per_site": 76,
+                 "clocks": clk16.summary()},
+        "error": {"vel_rel_l2_fp32_vs_fp64": err, "vel_rel_l2_fp16_vs_fp64": err16, "steps": args.err_steps},
         "e2e": {"value": round(e2e_mlups, 3), "unit": "MLUPS", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": round(e2e_ms, 4),
                 "api": "Solver.evolve(1) with page-locked host den/vel"},
