@@ -72,6 +72,8 @@ struct jlb_solver {
     double *red_partial = nullptr, *red_out = nullptr;
     int red_blocks = 0;
     double *fi_partial = nullptr, *fi_out = nullptr; // flow information (allocated on first use)
+    double *stg_den = nullptr, *stg_vel = nullptr;   // device copies of the host den/vel layout (DMA download)
+    bool stg_failed = false;
     // boundary-node tables (device)
     int M = 0, Mcap = 0;
     int64_t *d_sp_node = nullptr, *d_sp_rd = nullptr, *d_sp_wr = nullptr;
@@ -691,10 +693,55 @@ int run_steps(jlb_solver *s, uint32_t n, bool write_last) {
     return JLB_OK;
 }
 
+// copies the interior box of a halo-padded host array (comps doubles per
+// site) from its device copy with one pitched 3-D copy
+cudaError_t copy_interior(const jlb_solver *s, const double *src, double *dst, int comps) {
+    cudaMemcpy3DParms p{};
+    const size_t pitch = (size_t)s->NK * comps * sizeof(double);
+    p.srcPtr = make_cudaPitchedPtr((void *)src, pitch, (size_t)s->NK * comps * sizeof(double), s->NJ);
+    p.dstPtr = make_cudaPitchedPtr((void *)dst, pitch, (size_t)s->NK * comps * sizeof(double), s->NJ);
+    p.srcPos = make_cudaPos((size_t)comps * sizeof(double), 1, 1);
+    p.dstPos = p.srcPos;
+    p.extent = make_cudaExtent((size_t)s->nz * comps * sizeof(double), s->ny, s->nx);
+    p.kind = cudaMemcpyDeviceToHost;
+    return cudaMemcpy3DAsync(&p, s->st);
+}
+
+// Moments into the caller's page-locked den/vel.  When every interior site
+// is fluid, the FP64 rows are assembled in a device copy of the host layout
+// and moved by the copy engines in one pitched copy per array (the DMA path
+// sustains ~190 GB/s over NVLink-C2C against ~145 GB/s for kernel stores to
+// host memory); with solid sites, whose host values must stay untouched,
+// the kernel writes the fluid sites straight into host memory.
+// JLB_DMA_DOWNLOAD=0 keeps the kernel path.
 int download(jlb_solver *s, double *den, double *vel) {
     const size_t nb = (size_t)s->NCNT * sizeof(double);
     double *dd = (double *)dev_view(den);
     double *dv = (double *)dev_view(vel);
+    static const bool dma_off = [] {
+        const char *e = std::getenv("JLB_DMA_DOWNLOAD");
+        return e && e[0] == '0';
+    }();
+    if (dd && dv && !dma_off && s->nfluid == (uint64_t)s->N && !s->stg_failed) {
+        if (!s->stg_den) {
+            if (cudaMalloc(&s->stg_den, nb) != cudaSuccess || cudaMalloc(&s->stg_vel, 3 * nb) != cudaSuccess) {
+                cudaGetLastError();
+                cudaFree(s->stg_den);
+                s->stg_den = s->stg_vel = nullptr;
+                s->stg_failed = true;  // not enough device memory: kernel path from now on
+            }
+        }
+        if (s->stg_den) {
+            CKR(aux_download(s->prec, s->geom, s->nmask, s->mom[0], s->mom[1], s->mom[2], s->mom[3], s->stg_den,
+                             s->stg_vel, s->st));
+            CK(copy_interior(s, s->stg_den, den, 1));
+            CK(copy_interior(s, s->stg_vel, vel, 3));
+            s->d2h_bytes += s->nfluid * 4 * sizeof(double);
+            ++s->launches;
+            CK(cudaStreamSynchronize(s->st));
+            return JLB_OK;
+        }
+    }
     if (dd && dv) {
         CKR(aux_download(s->prec, s->geom, s->nmask, s->mom[0], s->mom[1], s->mom[2], s->mom[3], dd, dv, s->st));
         s->d2h_bytes += s->nfluid * 4 * sizeof(double);
@@ -859,7 +906,7 @@ void jlb_destroy(jlb_solver *s) {
     drop_graphs(s);
     void *bufs[] = {s->f, s->nmask, s->ncls, s->mom[0], s->mom[1], s->mom[2], s->mom[3], s->acc, s->red_partial,
                     s->red_out, s->d_sp_node, s->d_sp_info, s->d_sp_rd, s->d_sp_wr, s->d_sp_lw, s->d_sp_bc,
-                    s->d_sp_den, s->d_err, s->fi_partial, s->fi_out};
+                    s->d_sp_den, s->d_err, s->fi_partial, s->fi_out, s->stg_den, s->stg_vel};
     for (void *p : bufs)
         if (p) cudaFree(p);
     if (s->pinned) cudaFreeHost(s->pinned);
