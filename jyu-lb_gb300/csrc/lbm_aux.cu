@@ -207,10 +207,10 @@ constexpr int DL_TILE = 256;
 template <class C, bool SHIFTED>
 __global__ void __launch_bounds__(DL_TILE) download_kernel(AuxGeom g, int kchunks, const uint32_t *nmask,
                                                            const C *den, const C *ux, const C *uy, const C *uz,
-                                                           double *hden, double *hvel) {
+                                                           double *hden, double *hvel, int64_t row0) {
     __shared__ double sv[3 * DL_TILE];
     __shared__ unsigned char sfl[DL_TILE];
-    const int64_t rowc = blockIdx.x;
+    const int64_t rowc = blockIdx.x + row0 * kchunks;
     const int64_t row = rowc / kchunks;
     const int k0 = (int)(rowc - row * kchunks) * DL_TILE;
     const int i = (int)(row / g.ny), j = (int)(row - (int64_t)i * g.ny);
@@ -417,19 +417,26 @@ int aux_restore(int prec, const AuxGeom &g, void *f, const uint32_t *nmask, cons
     return (int)cudaGetLastError();
 }
 
-int aux_download(int prec, const AuxGeom &g, const uint32_t *nmask, const void *den, const void *ux,
-                 const void *uy, const void *uz, double *hden, double *hvel, cudaStream_t st) {
+int aux_download_rows(int prec, const AuxGeom &g, const uint32_t *nmask, const void *den, const void *ux,
+                      const void *uy, const void *uz, double *hden, double *hvel, int64_t row0, int64_t nrows,
+                      cudaStream_t st) {
     const int kchunks = (g.nz + DL_TILE - 1) / DL_TILE;
-    const unsigned b = (unsigned)((int64_t)g.nx * g.ny * kchunks);
+    const unsigned b = (unsigned)(nrows * kchunks);
+    if (b == 0) return 0;
     if (prec == PREC_FP64)
         download_kernel<double, false><<<b, DL_TILE, 0, st>>>(g, kchunks, nmask, (const double *)den,
                                                               (const double *)ux, (const double *)uy,
-                                                              (const double *)uz, hden, hvel);
+                                                              (const double *)uz, hden, hvel, row0);
     else
         download_kernel<float, true><<<b, DL_TILE, 0, st>>>(g, kchunks, nmask, (const float *)den,
                                                             (const float *)ux, (const float *)uy,
-                                                            (const float *)uz, hden, hvel);
+                                                            (const float *)uz, hden, hvel, row0);
     return (int)cudaGetLastError();
+}
+
+int aux_download(int prec, const AuxGeom &g, const uint32_t *nmask, const void *den, const void *ux,
+                 const void *uy, const void *uz, double *hden, double *hvel, cudaStream_t st) {
+    return aux_download_rows(prec, g, nmask, den, ux, uy, uz, hden, hvel, 0, (int64_t)g.nx * g.ny, st);
 }
 
 int aux_acc_upload(int prec, const AuxGeom &g, const double *hacc, void *acc, cudaStream_t st) {

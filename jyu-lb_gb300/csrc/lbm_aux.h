@@ -21,6 +21,10 @@ int aux_readout(int prec, const AuxGeom &g, const void *f, const uint32_t *nmask
                 const int64_t *sp_node, const int64_t *sp_wr, double *out, cudaStream_t st);
 int aux_restore(int prec, const AuxGeom &g, void *f, const uint32_t *nmask, const double *in, cudaStream_t st);
 // moments of fluid nodes into device-accessible halo-padded host arrays
+// rows [row0, row0 + nrows) of (i, j) rows only
+int aux_download_rows(int prec, const AuxGeom &g, const uint32_t *nmask, const void *den, const void *ux,
+                      const void *uy, const void *uz, double *hden, double *hvel, int64_t row0, int64_t nrows,
+                      cudaStream_t st);
 int aux_download(int prec, const AuxGeom &g, const uint32_t *nmask, const void *den, const void *ux,
                  const void *uy, const void *uz, double *hden, double *hvel, cudaStream_t st);
 // interior of a device-accessible halo-padded (NI,NJ,NK,3) array -> SoA field

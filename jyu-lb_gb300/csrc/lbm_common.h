@@ -59,6 +59,7 @@ struct StepArgs {
     // dense-node grid
     int bx, by, kblocks;  // block shape and k-blocks per row-block
     int nb_dense;         // number of dense blocks; the rest are boundary blocks
+    int b0;               // first dense block of this launch (a launch may cover a slab)
     // boundary (special) nodes
     int M;                // number of boundary nodes
     const int64_t *sp_node;

@@ -74,6 +74,8 @@ struct jlb_solver {
     double *fi_partial = nullptr, *fi_out = nullptr; // flow information (allocated on first use)
     double *stg_den = nullptr, *stg_vel = nullptr;   // device copies of the host den/vel layout (DMA download)
     bool stg_failed = false;
+    cudaStream_t st2 = nullptr;          // download stream of the overlapped last step
+    std::vector<cudaEvent_t> slab_ev;    // its slab events
     // boundary-node tables (device)
     int M = 0, Mcap = 0;
     int64_t *d_sp_node = nullptr, *d_sp_rd = nullptr, *d_sp_wr = nullptr;
@@ -636,6 +638,15 @@ int check_kernel_error(jlb_solver *s) {
     return JLB_OK;
 }
 
+// JLB_OVERLAP_DOWNLOAD=0 keeps the last step and the download in sequence
+bool overlap_off() {
+    static const bool off = [] {
+        const char *e = std::getenv("JLB_OVERLAP_DOWNLOAD");
+        return e && e[0] == '0';
+    }();
+    return off;
+}
+
 bool graphs_enabled() {
     static int en = -1;
     if (en < 0) {
@@ -693,54 +704,63 @@ int run_steps(jlb_solver *s, uint32_t n, bool write_last) {
     return JLB_OK;
 }
 
-// copies the interior box of a halo-padded host array (comps doubles per
-// site) from its device copy with one pitched 3-D copy
-cudaError_t copy_interior(const jlb_solver *s, const double *src, double *dst, int comps) {
+// copies planes [i0, i1) of the interior box of a halo-padded host array
+// (comps doubles per site) from its device copy with one pitched 3-D copy
+cudaError_t copy_interior(const jlb_solver *s, const double *src, double *dst, int comps, int i0, int i1,
+                          cudaStream_t st) {
     cudaMemcpy3DParms p{};
     const size_t pitch = (size_t)s->NK * comps * sizeof(double);
     p.srcPtr = make_cudaPitchedPtr((void *)src, pitch, (size_t)s->NK * comps * sizeof(double), s->NJ);
     p.dstPtr = make_cudaPitchedPtr((void *)dst, pitch, (size_t)s->NK * comps * sizeof(double), s->NJ);
-    p.srcPos = make_cudaPos((size_t)comps * sizeof(double), 1, 1);
+    p.srcPos = make_cudaPos((size_t)comps * sizeof(double), 1, 1 + (size_t)i0);
     p.dstPos = p.srcPos;
-    p.extent = make_cudaExtent((size_t)s->nz * comps * sizeof(double), s->ny, s->nx);
+    p.extent = make_cudaExtent((size_t)s->nz * comps * sizeof(double), s->ny, (size_t)(i1 - i0));
     p.kind = cudaMemcpyDeviceToHost;
-    return cudaMemcpy3DAsync(&p, s->st);
+    return cudaMemcpy3DAsync(&p, st);
 }
 
-// Moments into the caller's page-locked den/vel.  When every interior site
-// is fluid, the FP64 rows are assembled in a device copy of the host layout
-// and moved by the copy engines in one pitched copy per array (the DMA path
-// sustains ~190 GB/s over NVLink-C2C against ~145 GB/s for kernel stores to
-// host memory); with solid sites, whose host values must stay untouched,
-// the kernel writes the fluid sites straight into host memory.
-// JLB_DMA_DOWNLOAD=0 keeps the kernel path.
-int download(jlb_solver *s, double *den, double *vel) {
-    const size_t nb = (size_t)s->NCNT * sizeof(double);
-    double *dd = (double *)dev_view(den);
-    double *dv = (double *)dev_view(vel);
+// The copy-engine download applies when every interior site is fluid (the
+// host values of solid sites must stay untouched, so they cannot be
+// overwritten by a box copy) and den/vel are page-locked; it needs a device
+// copy of the host layout (allocated on first use).  JLB_DMA_DOWNLOAD=0
+// keeps the kernel path.
+bool dma_ready(jlb_solver *s, double *den, double *vel) {
     static const bool dma_off = [] {
         const char *e = std::getenv("JLB_DMA_DOWNLOAD");
         return e && e[0] == '0';
     }();
-    if (dd && dv && !dma_off && s->nfluid == (uint64_t)s->N && !s->stg_failed) {
-        if (!s->stg_den) {
-            if (cudaMalloc(&s->stg_den, nb) != cudaSuccess || cudaMalloc(&s->stg_vel, 3 * nb) != cudaSuccess) {
-                cudaGetLastError();
-                cudaFree(s->stg_den);
-                s->stg_den = s->stg_vel = nullptr;
-                s->stg_failed = true;  // not enough device memory: kernel path from now on
-            }
+    if (dma_off || s->stg_failed || s->nfluid != (uint64_t)s->N || !dev_view(den) || !dev_view(vel)) return false;
+    if (!s->stg_den) {
+        const size_t nb = (size_t)s->NCNT * sizeof(double);
+        if (cudaMalloc(&s->stg_den, nb) != cudaSuccess || cudaMalloc(&s->stg_vel, 3 * nb) != cudaSuccess) {
+            cudaGetLastError();
+            cudaFree(s->stg_den);
+            s->stg_den = s->stg_vel = nullptr;
+            s->stg_failed = true;  // not enough device memory: kernel path from now on
+            return false;
         }
-        if (s->stg_den) {
-            CKR(aux_download(s->prec, s->geom, s->nmask, s->mom[0], s->mom[1], s->mom[2], s->mom[3], s->stg_den,
-                             s->stg_vel, s->st));
-            CK(copy_interior(s, s->stg_den, den, 1));
-            CK(copy_interior(s, s->stg_vel, vel, 3));
-            s->d2h_bytes += s->nfluid * 4 * sizeof(double);
-            ++s->launches;
-            CK(cudaStreamSynchronize(s->st));
-            return JLB_OK;
-        }
+    }
+    return true;
+}
+
+// Moments into the caller's page-locked den/vel.  On the copy-engine path
+// the FP64 rows are assembled in a device copy of the host layout and moved
+// in one pitched copy per array (~190 GB/s over NVLink-C2C against ~145 GB/s
+// for kernel stores to host memory); otherwise the kernel writes the fluid
+// sites straight into host memory.
+int download(jlb_solver *s, double *den, double *vel) {
+    const size_t nb = (size_t)s->NCNT * sizeof(double);
+    double *dd = (double *)dev_view(den);
+    double *dv = (double *)dev_view(vel);
+    if (dma_ready(s, den, vel)) {
+        CKR(aux_download(s->prec, s->geom, s->nmask, s->mom[0], s->mom[1], s->mom[2], s->mom[3], s->stg_den,
+                         s->stg_vel, s->st));
+        CK(copy_interior(s, s->stg_den, den, 1, 0, s->nx, s->st));
+        CK(copy_interior(s, s->stg_vel, vel, 3, 0, s->nx, s->st));
+        s->d2h_bytes += s->nfluid * 4 * sizeof(double);
+        ++s->launches;
+        CK(cudaStreamSynchronize(s->st));
+        return JLB_OK;
     }
     if (dd && dv) {
         CKR(aux_download(s->prec, s->geom, s->nmask, s->mom[0], s->mom[1], s->mom[2], s->mom[3], dd, dv, s->st));
@@ -766,6 +786,65 @@ int download(jlb_solver *s, double *den, double *vel) {
     cudaFree(tden);
     cudaFree(tvel);
     return r;
+}
+
+// The last step of an evolve call with its download overlapped: the
+// boundary nodes first, then the dense sweep in slabs of i-planes, each slab
+// followed (on a second stream) by its FP64 assembly and its pitched copy to
+// the host while the next slab computes.  The direct step kernel runs this
+// step (the staged kernel's persistent grid does not split into slabs).
+// Used on the copy-engine download path when each slab is whole rows of
+// dense blocks (ny a multiple of the block's rows).
+int final_step_overlapped(jlb_solver *s, double *den, double *vel) {
+    const bool pstep = s->parity == 0;
+    StepArgs a = make_args(s, 1);
+    const int rows_per_block = a.by;
+    auto direct = [&](const StepArgs &x, int blocks) {
+        int r;
+        if (s->cfg.kernel == JLB_KERNEL_CXX) r = launch_step_cxx(x, s->cfg.rlx_scheme, s->cfg.kernel_opts, pstep, s->accf, blocks, s->st);
+        else if (s->prec == PREC_FP64) r = launch_step_fp64(x, s->cfg.rlx_scheme, pstep, s->accf, blocks, s->st);
+        else if (s->prec == PREC_FP32) r = launch_step_fp32(x, s->cfg.rlx_scheme, pstep, s->accf, blocks, s->st);
+        else r = launch_step_fp16(x, s->cfg.rlx_scheme, pstep, s->accf, blocks, s->st);
+        if (r) return fail(s, JLB_ERR_CUDA, std::string("step launch: ") + cudaGetErrorString((cudaError_t)r));
+        ++s->launches;
+        return JLB_OK;
+    };
+    if (!s->st2) CK(cudaStreamCreateWithFlags(&s->st2, cudaStreamNonBlocking));
+    const int nslab = std::min(8, s->nx);
+    while ((int)s->slab_ev.size() < nslab + 1) {
+        cudaEvent_t e;
+        CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        s->slab_ev.push_back(e);
+    }
+    int r;
+    if (a.M > 0) {
+        StepArgs sp = a;
+        sp.nb_dense = 0;
+        if ((r = direct(sp, (a.M + 127) / 128))) return r;
+    }
+    const int kb = a.kblocks;
+    for (int k = 0; k < nslab; ++k) {
+        const int i0 = (int)((int64_t)s->nx * k / nslab), i1 = (int)((int64_t)s->nx * (k + 1) / nslab);
+        if (i1 <= i0) continue;
+        StepArgs sl = a;
+        sl.M = 0;
+        sl.b0 = (int)((int64_t)i0 * s->ny / rows_per_block) * kb;
+        sl.nb_dense = (int)((int64_t)(i1 - i0) * s->ny / rows_per_block) * kb;
+        if ((r = direct(sl, sl.nb_dense))) return r;
+        CK(cudaEventRecord(s->slab_ev[k], s->st));
+        CK(cudaStreamWaitEvent(s->st2, s->slab_ev[k], 0));
+        CKR(aux_download_rows(s->prec, s->geom, s->nmask, s->mom[0], s->mom[1], s->mom[2], s->mom[3], s->stg_den,
+                              s->stg_vel, (int64_t)i0 * s->ny, (int64_t)(i1 - i0) * s->ny, s->st2));
+        CK(copy_interior(s, s->stg_den, den, 1, i0, i1, s->st2));
+        CK(copy_interior(s, s->stg_vel, vel, 3, i0, i1, s->st2));
+        ++s->launches;
+    }
+    s->parity ^= 1;
+    CK(cudaEventRecord(s->slab_ev[nslab], s->st2));
+    CK(cudaStreamWaitEvent(s->st, s->slab_ev[nslab], 0));
+    CK(cudaStreamSynchronize(s->st));
+    s->d2h_bytes += s->nfluid * 4 * sizeof(double);
+    return JLB_OK;
 }
 
 } // namespace
@@ -910,6 +989,8 @@ void jlb_destroy(jlb_solver *s) {
     for (void *p : bufs)
         if (p) cudaFree(p);
     if (s->pinned) cudaFreeHost(s->pinned);
+    for (cudaEvent_t e : s->slab_ev) cudaEventDestroy(e);
+    if (s->st2) { cudaStreamSynchronize(s->st2); cudaStreamDestroy(s->st2); }
     if (s->own_stream && s->st) cudaStreamDestroy(s->st);
     delete s;
 }
@@ -1059,11 +1140,12 @@ int jlb_evolve(jlb_solver *s, uint32_t tsteps, const double g[3], double *den, d
     t1 = clk::now();
     if (s->cfg.kernel == JLB_KERNEL_CXX && s->M > 0)
         return fail(s, JLB_ERR_UNSUPPORTED, "the C++-executable kernel has no moving solids");
-    r = run_steps(s, tsteps, true);
+    const bool overlap = !overlap_off() && dma_ready(s, den, vel) && s->ny % make_args(s, 0).by == 0;
+    r = run_steps(s, overlap ? tsteps - 1 : tsteps, !overlap);
     if (r) return r;
     s->host_t[3] += since(t1);
     t1 = clk::now();
-    r = download(s, den, vel);
+    r = overlap ? final_step_overlapped(s, den, vel) : download(s, den, vel);
     if (r) return r;
     if (s->use_tma && (r = check_kernel_error(s))) return r;
     s->host_t[4] += since(t1);

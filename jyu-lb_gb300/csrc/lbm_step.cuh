@@ -305,7 +305,7 @@ __device__ __forceinline__ void special_node(const StepArgs &a, int b) {
 template <class ST, class PH, bool PSTEP, bool ACCF, class IT>
 __global__ void __launch_bounds__(128, JLB_MIN_BLOCKS) lbm_step_kernel(const StepArgs a) {
     const int b = (int)blockIdx.x;
-    if (b < a.nb_dense) dense_node<ST, PH, PSTEP, ACCF, IT>(a, b);
+    if (b < a.nb_dense) dense_node<ST, PH, PSTEP, ACCF, IT>(a, b + a.b0);
     else special_node<ST, PH, PSTEP, ACCF>(a, b - a.nb_dense);
 }
 
