@@ -377,6 +377,36 @@ __global__ void flowinfo_final_kernel(const double *partial, int nblocks, double
 }
 
 // ---------------------------------------------------------------------------
+// fluid-only population layout: gather / scatter of the 19 slots of every
+// fluid site between the lattice layout (stride Np) and the fluid-only one
+// (stride Npc), and translation of the boundary-node element tables
+// ---------------------------------------------------------------------------
+template <class T>
+__global__ void sparse_pack_kernel(T *dense, T *comp, const int32_t *csite, int64_t Nc, int64_t Np,
+                                   int64_t Npc, int to_comp) {
+    const int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= Nc) return;
+    const int64_t n = csite[m];
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        if (to_comp) comp[q * Npc + m] = dense[q * Np + n];
+        else dense[q * Np + n] = comp[q * Npc + m];
+    }
+}
+
+__global__ void sparse_tables_kernel(const int64_t *rd, const int64_t *wr, const int64_t *node, int M,
+                                     const int32_t *cidx, int64_t Np, int64_t Npc, int64_t *rdc, int64_t *wrc,
+                                     int64_t *nodec) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e < (int64_t)Q * M) {
+        const int64_t r = rd[e], w = wr[e];
+        rdc[e] = (r / Np) * Npc + cidx[r % Np];
+        wrc[e] = (w / Np) * Npc + cidx[w % Np];
+    }
+    if (e < M) nodec[e] = cidx[node[e]];
+}
+
+// ---------------------------------------------------------------------------
 // host-callable launchers
 // ---------------------------------------------------------------------------
 static inline unsigned nblk(int64_t n, int t) { return (unsigned)((n + t - 1) / t); }
@@ -414,6 +444,26 @@ int aux_restore(int prec, const AuxGeom &g, void *f, const uint32_t *nmask, cons
     if (prec == PREC_FP64) restore_kernel<StoreF64><<<b, 128, 0, st>>>(g, (double *)f, nmask, in);
     else if (prec == PREC_FP32) restore_kernel<StoreF32><<<b, 128, 0, st>>>(g, (float *)f, nmask, in);
     else restore_kernel<StoreF16><<<b, 128, 0, st>>>(g, (__half *)f, nmask, in);
+    return (int)cudaGetLastError();
+}
+
+int aux_sparse_pack(int elem_bytes, void *dense, void *comp, const int32_t *csite, int64_t Nc, int64_t Np,
+                    int64_t Npc, int to_comp, cudaStream_t st) {
+    const unsigned b = nblk(Nc, 256);
+    if (b == 0) return 0;
+    if (elem_bytes == 8)
+        sparse_pack_kernel<uint64_t><<<b, 256, 0, st>>>((uint64_t *)dense, (uint64_t *)comp, csite, Nc, Np, Npc, to_comp);
+    else if (elem_bytes == 4)
+        sparse_pack_kernel<uint32_t><<<b, 256, 0, st>>>((uint32_t *)dense, (uint32_t *)comp, csite, Nc, Np, Npc, to_comp);
+    else
+        sparse_pack_kernel<uint16_t><<<b, 256, 0, st>>>((uint16_t *)dense, (uint16_t *)comp, csite, Nc, Np, Npc, to_comp);
+    return (int)cudaGetLastError();
+}
+
+int aux_sparse_tables(const int64_t *rd, const int64_t *wr, const int64_t *node, int M, const int32_t *cidx,
+                      int64_t Np, int64_t Npc, int64_t *rdc, int64_t *wrc, int64_t *nodec, cudaStream_t st) {
+    if (M <= 0) return 0;
+    sparse_tables_kernel<<<nblk((int64_t)Q * M, 256), 256, 0, st>>>(rd, wr, node, M, cidx, Np, Npc, rdc, wrc, nodec);
     return (int)cudaGetLastError();
 }
 

@@ -21,6 +21,14 @@ int aux_readout(int prec, const AuxGeom &g, const void *f, const uint32_t *nmask
                 const int64_t *sp_node, const int64_t *sp_wr, double *out, cudaStream_t st);
 int aux_restore(int prec, const AuxGeom &g, void *f, const uint32_t *nmask, const double *in, cudaStream_t st);
 // moments of fluid nodes into device-accessible halo-padded host arrays
+// fluid-only layout: copies the 19 slots of each fluid site between the
+// lattice layout (stride Np) and the fluid-only one (stride Npc); to_comp
+// selects the direction
+int aux_sparse_pack(int elem_bytes, void *dense, void *comp, const int32_t *csite, int64_t Nc, int64_t Np,
+                    int64_t Npc, int to_comp, cudaStream_t st);
+// boundary-node element tables (q * Np + n) -> fluid-only (q * Npc + m)
+int aux_sparse_tables(const int64_t *rd, const int64_t *wr, const int64_t *node, int M, const int32_t *cidx,
+                      int64_t Np, int64_t Npc, int64_t *rdc, int64_t *wrc, int64_t *nodec, cudaStream_t st);
 // rows [row0, row0 + nrows) of (i, j) rows only
 int aux_download_rows(int prec, const AuxGeom &g, const uint32_t *nmask, const void *den, const void *ux,
                       const void *uy, const void *uz, double *hden, double *hvel, int64_t row0, int64_t nrows,

@@ -60,6 +60,12 @@ struct StepArgs {
     int bx, by, kblocks;  // block shape and k-blocks per row-block
     int nb_dense;         // number of dense blocks; the rest are boundary blocks
     int b0;               // first dense block of this launch (a launch may cover a slab)
+    // fluid-only ("sparse") population layout, used on lattices with many
+    // solid sites: populations f[q * Npc + m] over the fluid sites m only
+    const int32_t *csite; // [Nc] lattice site n of fluid site m
+    const int32_t *cidx;  // [N] fluid index m of lattice site n (-1: solid)
+    int64_t Nc, Npc;      // fluid sites, their slot stride (multiple of 128)
+    const int64_t *sp_cnode; // [M] fluid index of each boundary node (sparse layout), else NULL
     // boundary (special) nodes
     int M;                // number of boundary nodes
     const int64_t *sp_node;
@@ -85,6 +91,10 @@ constexpr int CXX_FORCE2 = 2;    // second-order forcing term instead of the fir
 int launch_step_fp64(const StepArgs &a, int scheme, bool pstep, bool accf, int blocks, cudaStream_t st);
 int launch_step_fp32(const StepArgs &a, int scheme, bool pstep, bool accf, int blocks, cudaStream_t st);
 int launch_step_fp16(const StepArgs &a, int scheme, bool pstep, bool accf, int blocks, cudaStream_t st);
+// the same step on the fluid-only layout (a.csite/a.cidx set): blocks of 128
+// fluid sites, then the boundary-node blocks
+int launch_step_sparse_fp32(const StepArgs &a, int scheme, bool pstep, bool accf, int blocks, cudaStream_t st);
+int launch_step_sparse_fp16(const StepArgs &a, int scheme, bool pstep, bool accf, int blocks, cudaStream_t st);
 // the C++-executable collision model (lbm_cxx.cu), FP64; opts: CXX_* flags
 int launch_step_cxx(const StepArgs &a, int scheme, int opts, bool pstep, bool accf, int blocks, cudaStream_t st);
 // bulk-copy staged variants (lbm_step_tma.cuh): persistent grid over

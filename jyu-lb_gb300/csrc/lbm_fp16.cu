@@ -24,4 +24,8 @@ int tma_blocks_per_sm_fp16(int scheme) {
     return e == cudaSuccess ? nb : 0;
 }
 
+int launch_step_sparse_fp16(const StepArgs &a, int scheme, bool pstep, bool accf, int blocks, cudaStream_t st) {
+    return launch_step_sparse_impl<StoreF16, PhysSh>(a, scheme, pstep, accf, blocks, st);
+}
+
 } // namespace jlb

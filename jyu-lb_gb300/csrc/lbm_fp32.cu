@@ -25,4 +25,8 @@ int tma_blocks_per_sm_fp32(int scheme) {
     return e == cudaSuccess ? nb : 0;
 }
 
+int launch_step_sparse_fp32(const StepArgs &a, int scheme, bool pstep, bool accf, int blocks, cudaStream_t st) {
+    return launch_step_sparse_impl<StoreF32, PhysSh>(a, scheme, pstep, accf, blocks, st);
+}
+
 } // namespace jlb

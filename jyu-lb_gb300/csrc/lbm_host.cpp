@@ -75,6 +75,16 @@ struct jlb_solver {
     double *stg_den = nullptr, *stg_vel = nullptr;   // device copies of the host den/vel layout (DMA download)
     bool stg_failed = false;
     cudaStream_t st2 = nullptr;          // download stream of the overlapped last step
+    // fluid-only population layout (lattices with many solid sites)
+    bool sparse = false;                 // chosen at finalize_init
+    bool no_sparse = false;              // the adjoint driver keeps the lattice layout
+    bool c_current = false;              // the fluid-only copy holds the current state
+    bool sp_tables_dirty = true;         // boundary tables changed since their translation
+    void *fc = nullptr;                  // [19][Npc] populations of the fluid sites
+    int32_t *d_csite = nullptr, *d_cidx = nullptr;
+    int64_t *d_sp_rd_c = nullptr, *d_sp_wr_c = nullptr, *d_sp_cnode = nullptr;
+    int sp_c_cap = 0;
+    int64_t Nc = 0, Npc = 0;
     std::vector<cudaEvent_t> slab_ev;    // its slab events
     // boundary-node tables (device)
     int M = 0, Mcap = 0;
@@ -502,6 +512,7 @@ void drop_graphs(jlb_solver *s) {
 // uploads the static boundary tables (after build_special)
 int upload_tables(jlb_solver *s) {
     const int M = s->M;
+    s->sp_tables_dirty = true;
     if (M > s->Mcap) {
         const size_t cap = (size_t)M + M / 4 + 64;
         int r;
@@ -577,6 +588,16 @@ StepArgs make_args(const jlb_solver *s, int write_moments) {
     a.sp_lw = s->d_sp_lw; a.sp_bc = s->d_sp_bc;
     a.sp_den = s->d_sp_den;
     for (int f = 0; f < 6; ++f) a.bc[f] = s->cfg.bc[f];
+    if (s->sparse && s->fc) {
+        a.f = s->fc;
+        a.csite = s->d_csite;
+        a.cidx = s->d_cidx;
+        a.Nc = s->Nc;
+        a.Npc = s->Npc;
+        a.sp_rd = s->d_sp_rd_c;
+        a.sp_wr = s->d_sp_wr_c;
+        a.sp_cnode = s->d_sp_cnode;
+    }
     return a;
 }
 
@@ -584,7 +605,11 @@ int launch_one(jlb_solver *s, const StepArgs &a, bool pstep) {
     const int blocks = a.nb_dense + (a.M + 127) / 128;
     const int nsb = (a.M + 127) / 128;
     int r;
-    if (s->use_tma && !a.fout && !a.sp_tee && (s->tma_p || !pstep)) {
+    if (a.csite) {
+        const int nb = (int)((a.Nc + 127) / 128) + nsb;
+        if (s->prec == PREC_FP32) r = launch_step_sparse_fp32(a, s->cfg.rlx_scheme, pstep, s->accf, nb, s->st);
+        else r = launch_step_sparse_fp16(a, s->cfg.rlx_scheme, pstep, s->accf, nb, s->st);
+    } else if (s->use_tma && !a.fout && !a.sp_tee && (s->tma_p || !pstep)) {
         const int ntiles = a.nb_dense; // one 128-site tile per dense block (bx = 128, by = 1)
         if (s->prec == PREC_FP32)
             r = launch_step_tma_fp32(a, s->cfg.rlx_scheme, pstep, s->accf, s->tma_grid, ntiles, nsb, s->d_err, s->st);
@@ -609,6 +634,16 @@ int launch_one(jlb_solver *s, const StepArgs &a, bool pstep) {
 // staging, JLB_TMA=1 stages both steps.
 void choose_kernel(jlb_solver *s) {
     s->use_tma = false;
+    // fluid-only layout for FP32 / FP16 storage when under 80% of the sites
+    // are fluid: a lattice-ordered sweep then fetches population lines that
+    // are partly solid slots (1.6x the fluid bytes at porosity 0.6).
+    // JLB_SPARSE=0 keeps the lattice layout, JLB_SPARSE=1 forces the other.
+    const char *es = std::getenv("JLB_SPARSE");
+    s->sparse = !s->no_sparse && s->prec != PREC_FP64 && s->cfg.kernel == JLB_KERNEL_JYULB &&
+                s->N < (int64_t)1 << 31 &&
+                ((es && es[0]) ? es[0] == '1' : (double)s->nfluid < 0.8 * (double)s->N);
+    s->c_current = false;
+    if (s->sparse) { ++s->args_version; return; }
     const char *e = std::getenv("JLB_TMA");
     if (e && e[0] == '0') return;
     s->tma_p = e && e[0] == '1';
@@ -657,8 +692,78 @@ bool graphs_enabled() {
 }
 
 // runs n steps; the last one writes moments when write_last
+// builds the fluid-only layout on first use: site lists from the node mask
+int sparse_setup(jlb_solver *s) {
+    if (s->fc) return JLB_OK;
+    std::vector<uint32_t> mask((size_t)s->N);
+    CK(cudaMemcpy(mask.data(), s->nmask, (size_t)s->N * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    std::vector<int32_t> cidx((size_t)s->N, -1), csite;
+    csite.reserve((size_t)s->nfluid);
+    for (int64_t n = 0; n < s->N; ++n)
+        if (!(mask[n] & MASK_SOLID)) { cidx[n] = (int32_t)csite.size(); csite.push_back((int32_t)n); }
+    s->Nc = (int64_t)csite.size();
+    s->Npc = ((s->Nc + 127) / 128) * 128;
+    if (cudaMalloc(&s->fc, (size_t)19 * s->Npc * s->ssz) != cudaSuccess ||
+        cudaMalloc(&s->d_csite, std::max<size_t>(1, csite.size()) * sizeof(int32_t)) != cudaSuccess ||
+        cudaMalloc(&s->d_cidx, (size_t)s->N * sizeof(int32_t)) != cudaSuccess) {
+        cudaGetLastError();
+        cudaFree(s->fc); cudaFree(s->d_csite); cudaFree(s->d_cidx);
+        s->fc = nullptr; s->d_csite = s->d_cidx = nullptr;
+        s->sparse = false;  // not enough device memory: lattice layout
+        ++s->args_version;
+        return JLB_OK;
+    }
+    CK(cudaMemcpy(s->d_csite, csite.data(), csite.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(s->d_cidx, cidx.data(), cidx.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+    s->sp_tables_dirty = true;
+    ++s->args_version;
+    return JLB_OK;
+}
+
+// makes the fluid-only copy current (gathering the lattice copy if needed)
+// and its boundary tables up to date
+int sparse_enter(jlb_solver *s) {
+    int r = sparse_setup(s);
+    if (r || !s->sparse) return r;
+    if (s->sp_tables_dirty && s->M > 0) {
+        if (s->M > s->sp_c_cap) {
+            cudaFree(s->d_sp_rd_c); cudaFree(s->d_sp_wr_c); cudaFree(s->d_sp_cnode);
+            const int cap = s->M + s->M / 4 + 64;
+            s->d_sp_rd_c = s->d_sp_wr_c = s->d_sp_cnode = nullptr;
+            CK(cudaMalloc(&s->d_sp_rd_c, (size_t)19 * cap * sizeof(int64_t)));
+            CK(cudaMalloc(&s->d_sp_wr_c, (size_t)19 * cap * sizeof(int64_t)));
+            CK(cudaMalloc(&s->d_sp_cnode, (size_t)cap * sizeof(int64_t)));
+            s->sp_c_cap = cap;
+            ++s->args_version;
+        }
+        CKR(aux_sparse_tables(s->d_sp_rd, s->d_sp_wr, s->d_sp_node, s->M, s->d_cidx, s->Np, s->Npc, s->d_sp_rd_c,
+                              s->d_sp_wr_c, s->d_sp_cnode, s->st));
+        ++s->launches;
+    }
+    s->sp_tables_dirty = false;
+    if (!s->c_current) {
+        CKR(aux_sparse_pack((int)s->ssz, s->f, s->fc, s->d_csite, s->Nc, s->Np, s->Npc, 1, s->st));
+        ++s->launches;
+        s->c_current = true;
+    }
+    return JLB_OK;
+}
+
+// makes the lattice-layout copy current (for population read-out / writes)
+int sparse_leave(jlb_solver *s) {
+    if (!s->sparse || !s->fc || !s->c_current) return JLB_OK;
+    CKR(aux_sparse_pack((int)s->ssz, s->f, s->fc, s->d_csite, s->Nc, s->Np, s->Npc, 0, s->st));
+    ++s->launches;
+    s->c_current = false;
+    return JLB_OK;
+}
+
 int run_steps(jlb_solver *s, uint32_t n, bool write_last) {
     if (n == 0) return JLB_OK;
+    if (s->sparse) {
+        int r = sparse_enter(s);
+        if (r) return r;
+    }
     const StepArgs a0 = make_args(s, 0);
     uint32_t plain = write_last ? n - 1 : n;
     if (graphs_enabled() && plain >= (uint32_t)s->GK) {
@@ -985,7 +1090,8 @@ void jlb_destroy(jlb_solver *s) {
     drop_graphs(s);
     void *bufs[] = {s->f, s->nmask, s->ncls, s->mom[0], s->mom[1], s->mom[2], s->mom[3], s->acc, s->red_partial,
                     s->red_out, s->d_sp_node, s->d_sp_info, s->d_sp_rd, s->d_sp_wr, s->d_sp_lw, s->d_sp_bc,
-                    s->d_sp_den, s->d_err, s->fi_partial, s->fi_out, s->stg_den, s->stg_vel};
+                    s->d_sp_den, s->d_err, s->fi_partial, s->fi_out, s->stg_den, s->stg_vel,
+                    s->fc, s->d_csite, s->d_cidx, s->d_sp_rd_c, s->d_sp_wr_c, s->d_sp_cnode};
     for (void *p : bufs)
         if (p) cudaFree(p);
     if (s->pinned) cudaFreeHost(s->pinned);
@@ -1140,7 +1246,7 @@ int jlb_evolve(jlb_solver *s, uint32_t tsteps, const double g[3], double *den, d
     t1 = clk::now();
     if (s->cfg.kernel == JLB_KERNEL_CXX && s->M > 0)
         return fail(s, JLB_ERR_UNSUPPORTED, "the C++-executable kernel has no moving solids");
-    const bool overlap = !overlap_off() && dma_ready(s, den, vel) && s->ny % make_args(s, 0).by == 0;
+    const bool overlap = !overlap_off() && !s->sparse && dma_ready(s, den, vel) && s->ny % make_args(s, 0).by == 0;
     r = run_steps(s, overlap ? tsteps - 1 : tsteps, !overlap);
     if (r) return r;
     s->host_t[3] += since(t1);
@@ -1177,6 +1283,8 @@ int jlb_get_populations(jlb_solver *s, double *f) {
     if (!s || !f) return fail(s, JLB_ERR_INVALID_ARG, "NULL argument");
     if (!s->init_done) return fail(s, JLB_ERR_STATE, "finalize_init has not been called");
     const size_t nb = (size_t)19 * s->N * sizeof(double);
+    int r0 = sparse_leave(s);
+    if (r0) return r0;
     double *tmp = nullptr;
     CK(cudaMalloc(&tmp, nb));
     int r = aux_readout(s->prec, s->geom, s->f, s->nmask, s->parity, s->M, s->d_sp_node, s->d_sp_wr, tmp, s->st);
@@ -1196,6 +1304,7 @@ int jlb_set_populations(jlb_solver *s, const double *f) {
     CK(cudaMalloc(&tmp, nb));
     cudaError_t e = cudaMemcpyAsync(tmp, f, nb, cudaMemcpyHostToDevice, s->st);
     if (e == cudaSuccess) e = (cudaError_t)aux_restore(s->prec, s->geom, s->f, s->nmask, tmp, s->st);
+    s->c_current = false;  // the lattice copy is current again
     ++s->launches;
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
     cudaFree(tmp);
@@ -1817,6 +1926,7 @@ int jlb_adj_create(const jlb_config *cfg, const uint8_t *phase, int32_t loss_pla
     int r = jlb_create(cfg, &A->s);
     if (r) { std::string m = g_create_error; delete A; return afail(nullptr, r, m); }
     jlb_solver *s = A->s;
+    s->no_sparse = true;  // checkpoints and recomputation work on the lattice layout
     // rest state: den = 1, vel = 0 everywhere, so the initial populations do
     // not depend on the parameters
     std::vector<uint8_t> ph((size_t)s->NCNT, 0);

@@ -229,12 +229,15 @@ __device__ __forceinline__ void special_node(const StepArgs &a, int b) {
     const uint32_t info = __ldg(a.sp_info + t);
     S *__restrict__ f = (S *)a.f;
     const int64_t Np = a.Np;
+    // population slots of the node: lattice layout, or the fluid-only layout
+    const int64_t pn = a.sp_cnode ? __ldg(a.sp_cnode + t) : n;
+    const int64_t PNp = a.sp_cnode ? a.Npc : Np;
     C *spden = (C *)a.sp_den;
     const C dprev = spden[t];
     C fv[Q];
 
     Unroll<0, Q>::run([&]<int q>() {
-        const int64_t addr = PSTEP ? __ldg(a.sp_rd + (int64_t)q * M + t) : (int64_t)q * Np + n;
+        const int64_t addr = PSTEP ? __ldg(a.sp_rd + (int64_t)q * M + t) : (int64_t)q * PNp + pn;
         // the value read may belong to any slot; decode with the slot of q's
         // source population (same weight class: mirrors and opposites keep it)
         C v = ST::template ld<q>(f + addr);
@@ -287,10 +290,81 @@ __device__ __forceinline__ void special_node(const StepArgs &a, int b) {
             const int64_t addr = __ldg(a.sp_wr + (int64_t)q * M + t);
             ST::template st<q>(fo + addr, fv[q]);
         } else {
-            ST::template st<OPP(q)>(fo + OPP(q) * Np + n, fv[q]);
+            ST::template st<OPP(q)>(fo + OPP(q) * PNp + pn, fv[q]);
         }
     });
     spden[t] = rho;
+    if (a.write_moments) {
+        ((C *)a.den)[n] = rho;
+        ((C *)a.ux)[n] = ux;
+        ((C *)a.uy)[n] = uy;
+        ((C *)a.uz)[n] = uz;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// fluid sites on the fluid-only layout.  On porous lattices a lattice-ordered
+// sweep fetches whole population lines that are partly solid slots; here the
+// populations of fluid sites are packed (f[q * Npc + m]) and a neighbour's
+// slot is found through the lattice-to-fluid index map (cidx, 4 bytes per
+// lattice site, cached), so only fluid populations move.  Same arithmetic and
+// AA pattern as dense_node.
+// ---------------------------------------------------------------------------
+template <class ST, class PH, bool PSTEP, bool ACCF>
+__device__ __forceinline__ void sparse_node(const StepArgs &a, int b) {
+    using S = typename ST::S;
+    using C = typename ST::C;
+    const int64_t m = (int64_t)b * (blockDim.x * blockDim.y) + (threadIdx.y * blockDim.x + threadIdx.x);
+    if (m >= a.Nc) return;
+    const int32_t n = __ldg(a.csite + m);
+    const uint8_t cls = __ldg(a.ncls + n);
+    if (cls >= CLS_SPECIAL) return;
+    const uint32_t mk = (PSTEP && cls == CLS_WALL) ? __ldg(a.nmask + n) : 0u;
+    S *__restrict__ f = (S *)a.f;
+    const int64_t Npc = a.Npc;
+    int32_t dI[3], dJ[3], dK[3];
+    if (PSTEP) {
+        const int32_t syz = a.ny * a.nz;
+        const int32_t i = n / syz, r = n - i * syz, j = r / a.nz, k = r - j * a.nz;
+        dI[0] = (i == 0 ? (a.nx - 1) : -1) * syz; dI[1] = 0; dI[2] = (i + 1 == a.nx ? (1 - a.nx) : 1) * syz;
+        dJ[0] = (j == 0 ? (a.ny - 1) : -1) * a.nz; dJ[1] = 0; dJ[2] = (j + 1 == a.ny ? (1 - a.ny) : 1) * a.nz;
+        dK[0] = k == 0 ? (a.nz - 1) : -1; dK[1] = 0; dK[2] = k + 1 == a.nz ? (1 - a.nz) : 1;
+    }
+    // fluid index of the neighbour across link q (site x + c_q); only asked
+    // for links that do not bounce back, whose neighbour is fluid
+    auto nbr = [&]<int q>() -> int64_t {
+        return __ldg(a.cidx + (n + dI[1 + CX(q)] + dJ[1 + CY(q)] + dK[1 + CZ(q)]));
+    };
+    C fv[Q];
+    Unroll<0, Q>::run([&]<int q>() {
+        int64_t e;
+        if (!PSTEP || q == 9) e = (int64_t)q * Npc + m;
+        else if (mk & (1u << q)) e = (int64_t)q * Npc + m;
+        else e = (int64_t)OPP(q) * Npc + nbr.template operator()<OPP(q)>();
+        fv[q] = ST::template ld<q>(f + e);
+    });
+    C ux, uy, uz;
+    C ax, ay, az;
+    if (ACCF) {
+        const C *acc = (const C *)a.acc;
+        ax = (C)a.g[0] + __ldg(acc + n);
+        ay = (C)a.g[1] + __ldg(acc + a.Np + n);
+        az = (C)a.g[2] + __ldg(acc + 2 * a.Np + n);
+    } else {
+        ax = (C)a.g[0]; ay = (C)a.g[1]; az = (C)a.g[2];
+    }
+    const C rho = PH::collide(fv, ax, ay, az, (C)a.w_e, (C)a.w_o, ux, uy, uz);
+    Unroll<0, Q>::run([&]<int q>() {
+        if (!PSTEP) {
+            ST::template st<OPP(q)>(f + ((int64_t)OPP(q) * Npc + m), fv[q]);
+            return;
+        }
+        int64_t e;
+        if (q == 9) e = 9 * Npc + m;
+        else if (mk & (1u << OPP(q))) e = (int64_t)OPP(q) * Npc + m;
+        else e = (int64_t)q * Npc + nbr.template operator()<q>();
+        ST::template st<q>(f + e, fv[q]);
+    });
     if (a.write_moments) {
         ((C *)a.den)[n] = rho;
         ((C *)a.ux)[n] = ux;
@@ -307,6 +381,28 @@ __global__ void __launch_bounds__(128, JLB_MIN_BLOCKS) lbm_step_kernel(const Ste
     const int b = (int)blockIdx.x;
     if (b < a.nb_dense) dense_node<ST, PH, PSTEP, ACCF, IT>(a, b + a.b0);
     else special_node<ST, PH, PSTEP, ACCF>(a, b - a.nb_dense);
+}
+
+template <class ST, class PH, bool PSTEP, bool ACCF>
+__global__ void __launch_bounds__(128, JLB_MIN_BLOCKS) lbm_step_sparse_kernel(const StepArgs a) {
+    const int b = (int)blockIdx.x;
+    const int nbc = (int)((a.Nc + 127) / 128);
+    if (b < nbc) sparse_node<ST, PH, PSTEP, ACCF>(a, b);
+    else special_node<ST, PH, PSTEP, ACCF>(a, b - nbc);
+}
+
+template <class ST, template <int> class PH>
+int launch_step_sparse_impl(const StepArgs &a, int scheme, bool pstep, bool accf, int blocks, cudaStream_t st) {
+#define JLB_SL(SCH, P, A) lbm_step_sparse_kernel<ST, PH<SCH>, P, A><<<blocks, 128, 0, st>>>(a)
+#define JLB_SS(SCH)                                                          \
+    if (pstep) { if (accf) JLB_SL(SCH, true, true); else JLB_SL(SCH, true, false); } \
+    else { if (accf) JLB_SL(SCH, false, true); else JLB_SL(SCH, false, false); }
+    if (scheme == SCH_BGK) { JLB_SS(SCH_BGK) }
+    else if (scheme == SCH_TRT) { JLB_SS(SCH_TRT) }
+    else { JLB_SS(SCH_REG) }
+#undef JLB_SS
+#undef JLB_SL
+    return (int)cudaGetLastError();
 }
 
 template <class ST, template <int> class PH>
