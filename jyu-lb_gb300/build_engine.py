@@ -23,10 +23,11 @@ COMMON = ["-std=c++20", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler",
           "-I", CSRC, "-I", INCLUDE]
 UNITS = {
     "lbm_fp64.cu": ["-fmad=false"],
-    # 6 resident 128-thread blocks per SM (<= 80 registers): the FP32/FP16
-    # steps are latency-bound on HBM at lower occupancy
-    "lbm_fp32.cu": ["-DJLB_MIN_BLOCKS=6"],
-    "lbm_fp16.cu": ["-DJLB_MIN_BLOCKS=6"],
+    # 8 resident 128-thread blocks per SM (<= 64 registers): the FP32/FP16
+    # steps are latency-bound on HBM, and 32 warps per SM keep more loads in
+    # flight than 24 (measured faster at 256^3 even where a few registers spill)
+    "lbm_fp32.cu": ["-DJLB_MIN_BLOCKS=8"],
+    "lbm_fp16.cu": ["-DJLB_MIN_BLOCKS=8"],
     "lbm_aux.cu": ["-fmad=false"],
     "lbm_noalloc.cu": [],
     "lbm_batch.cu": [],

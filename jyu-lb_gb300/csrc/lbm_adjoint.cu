@@ -287,7 +287,17 @@ template <class C> __device__ __forceinline__ void block_sensitivities(C *pg, do
 // resident blocks per SM the dense kernel is compiled for: the FP32 sweep
 // fits 5 x 128 threads (<= 96 registers) without spills; the loss-seeding
 // variant, which runs once per sweep, gets 4
-template <class ST, bool SEED> constexpr int adj_min_blocks() { return ST::shifted ? (SEED ? 4 : 5) : 1; }
+// resident 128-thread blocks per SM asked of the register allocator (the
+// seeding launch, which also forms the loss gradient, gets one fewer)
+#ifndef JLB_ADJ_MIN_BLOCKS
+#define JLB_ADJ_MIN_BLOCKS 6
+#endif
+#ifndef JLB_ADJ_MIN_BLOCKS_SEED
+#define JLB_ADJ_MIN_BLOCKS_SEED 5
+#endif
+template <class ST, bool SEED> constexpr int adj_min_blocks() {
+    return ST::shifted ? (SEED ? JLB_ADJ_MIN_BLOCKS_SEED : JLB_ADJ_MIN_BLOCKS) : 1;
+}
 
 // Dense sites.  Their collision inputs are gathered from the state before the
 // step (A.snap) exactly as the forward step gathers them; the adjoint of the

@@ -26,8 +26,14 @@ __device__ __forceinline__ int32_t split_div(int32_t l, int32_t d, float inv, in
     return q;
 }
 
+// resident warps per SM asked of the register allocator: the P step is
+// latency-bound, and 32 warps beat 24 on the 512-channel ensemble although
+// the P step then spills a few registers
+#ifndef JLB_BATCH_WARPS
+#define JLB_BATCH_WARPS 32
+#endif
 template <int SCH, bool PSTEP, int BLOCK>
-__global__ void __launch_bounds__(BLOCK, (BLOCK >= 256 ? 3 : BLOCK >= 128 ? 6 : 12))
+__global__ void __launch_bounds__(BLOCK, JLB_BATCH_WARPS * 32 / BLOCK)
     lbm_batch_kernel(const BatchArgs a) {
     using ST = StoreF32;
     using PH = PhysSh<SCH>;

@@ -373,18 +373,29 @@ __device__ __forceinline__ void sparse_node(const StepArgs &a, int b) {
     }
 }
 
+// resident 128-thread blocks per SM asked of the register allocator, per
+// kernel kind (the build sets them per storage type)
 #ifndef JLB_MIN_BLOCKS
 #define JLB_MIN_BLOCKS 1
 #endif
+#ifndef JLB_MIN_BLOCKS_STEP
+#define JLB_MIN_BLOCKS_STEP JLB_MIN_BLOCKS
+#endif
+#ifndef JLB_MIN_BLOCKS_TMA
+#define JLB_MIN_BLOCKS_TMA JLB_MIN_BLOCKS
+#endif
+#ifndef JLB_MIN_BLOCKS_SPARSE
+#define JLB_MIN_BLOCKS_SPARSE JLB_MIN_BLOCKS
+#endif
 template <class ST, class PH, bool PSTEP, bool ACCF, class IT>
-__global__ void __launch_bounds__(128, JLB_MIN_BLOCKS) lbm_step_kernel(const StepArgs a) {
+__global__ void __launch_bounds__(128, JLB_MIN_BLOCKS_STEP) lbm_step_kernel(const StepArgs a) {
     const int b = (int)blockIdx.x;
     if (b < a.nb_dense) dense_node<ST, PH, PSTEP, ACCF, IT>(a, b + a.b0);
     else special_node<ST, PH, PSTEP, ACCF>(a, b - a.nb_dense);
 }
 
 template <class ST, class PH, bool PSTEP, bool ACCF>
-__global__ void __launch_bounds__(128, JLB_MIN_BLOCKS) lbm_step_sparse_kernel(const StepArgs a) {
+__global__ void __launch_bounds__(128, JLB_MIN_BLOCKS_SPARSE) lbm_step_sparse_kernel(const StepArgs a) {
     const int b = (int)blockIdx.x;
     const int nbc = (int)((a.Nc + 127) / 128);
     if (b < nbc) sparse_node<ST, PH, PSTEP, ACCF>(a, b);

@@ -107,7 +107,7 @@ __device__ __forceinline__ void tma_issue(const StepArgs &a, int tile, S *buf, u
 }
 
 template <class ST, class PH, bool PSTEP, bool ACCF>
-__global__ void __launch_bounds__(128, JLB_MIN_BLOCKS) lbm_step_tma_kernel(const StepArgs a, int ntiles,
+__global__ void __launch_bounds__(128, JLB_MIN_BLOCKS_TMA) lbm_step_tma_kernel(const StepArgs a, int ntiles,
                                                                             int nspecial_blocks, int *err) {
     using S = typename ST::S;
     using C = typename ST::C;
