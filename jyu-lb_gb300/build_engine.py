@@ -23,10 +23,12 @@ COMMON = ["-std=c++20", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler",
           "-I", CSRC, "-I", INCLUDE]
 UNITS = {
     "lbm_fp64.cu": ["-fmad=false"],
-    # 8 resident 128-thread blocks per SM (<= 64 registers): the FP32/FP16
-    # steps are latency-bound on HBM, and 32 warps per SM keep more loads in
-    # flight than 24 (measured faster at 256^3 even where a few registers spill)
-    "lbm_fp32.cu": ["-DJLB_MIN_BLOCKS=8"],
+    # resident 128-thread blocks per SM.  The direct steps are latency-bound
+    # on HBM: 8 blocks (<= 64 registers, 32 warps) keep more loads in flight
+    # than 6 or 7, even where a few registers spill.  The persistent staged L
+    # step keeps its loads in flight as bulk copies and runs fastest at 5
+    # blocks for FP32 and 8 for FP16 (sweeps of 4..9 on the 256^3 cavity).
+    "lbm_fp32.cu": ["-DJLB_MIN_BLOCKS=8", "-DJLB_MIN_BLOCKS_TMA=5"],
     "lbm_fp16.cu": ["-DJLB_MIN_BLOCKS=8"],
     "lbm_aux.cu": ["-fmad=false"],
     "lbm_noalloc.cu": [],
