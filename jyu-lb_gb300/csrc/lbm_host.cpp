@@ -895,7 +895,7 @@ int download(jlb_solver *s, double *den, double *vel) {
 
 // The last step of an evolve call with its download overlapped: the
 // boundary nodes first, then the dense sweep in slabs of i-planes, each slab
-// followed (on a second stream) by its FP64 assembly and its pitched copy to
+// followed by its FP64 assembly and (on a second stream) its pitched copy to
 // the host while the next slab computes.  The direct step kernel runs this
 // step (the staged kernel's persistent grid does not split into slabs).
 // Used on the copy-engine download path when each slab is whole rows of
@@ -936,10 +936,12 @@ int final_step_overlapped(jlb_solver *s, double *den, double *vel) {
         sl.b0 = (int)((int64_t)i0 * s->ny / rows_per_block) * kb;
         sl.nb_dense = (int)((int64_t)(i1 - i0) * s->ny / rows_per_block) * kb;
         if ((r = direct(sl, sl.nb_dense))) return r;
+        // the slab's FP64 assembly follows its step on the compute stream, so
+        // that the copy stream carries nothing but back-to-back copies
+        CKR(aux_download_rows(s->prec, s->geom, s->nmask, s->mom[0], s->mom[1], s->mom[2], s->mom[3], s->stg_den,
+                              s->stg_vel, (int64_t)i0 * s->ny, (int64_t)(i1 - i0) * s->ny, s->st));
         CK(cudaEventRecord(s->slab_ev[k], s->st));
         CK(cudaStreamWaitEvent(s->st2, s->slab_ev[k], 0));
-        CKR(aux_download_rows(s->prec, s->geom, s->nmask, s->mom[0], s->mom[1], s->mom[2], s->mom[3], s->stg_den,
-                              s->stg_vel, (int64_t)i0 * s->ny, (int64_t)(i1 - i0) * s->ny, s->st2));
         CK(copy_interior(s, s->stg_den, den, 1, i0, i1, s->st2));
         CK(copy_interior(s, s->stg_vel, vel, 3, i0, i1, s->st2));
         ++s->launches;
