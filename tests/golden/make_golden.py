@@ -8,7 +8,7 @@ last call: post-collision populations decoded from Solver.f1's Bundle-C layout
 (jyulb/isothermal.pyx:1532-1704) into (19, nx, ny, nz), and the interior den
 and vel.  Run from the repository root:
 
-    python oracle/build_ref.py && python tests/golden/make_golden.py
+    python oracle/build_ref.py && python tests/golden/make_golden.py [case ...]
 """
 from __future__ import annotations
 
@@ -119,6 +119,35 @@ def cases():
     out.append(dict(name="invel_grav", lat=list(sh), scheme=TRT, kvisc=0.08, g=[2e-5, 0, 0],
                     bc=[FV, FD, WALL, WALL, PER, PER], phase=ph, den=np.ones(sh), vel=vel, acc=None,
                     chunks=[10, 10, 10]))
+    # degenerate shapes: one site periodic on every axis (each link wraps
+    # onto the site itself)
+    rng = np.random.default_rng(21)
+    sh = (1, 1, 1)
+    out.append(dict(name="edge_single_site", lat=list(sh), scheme=TRT, kvisc=0.07,
+                    g=[3e-5, -1e-5, 2e-5], bc=[PER] * 6, phase=np.ones(sh, np.uint8),
+                    den=np.full(sh, 1.02), vel=0.01 * rng.standard_normal(sh + (3,)), acc=None,
+                    chunks=[3, 4]))
+    # a single column along z (nz > 128, not a multiple of 32): symmetric x,
+    # periodic y, wall below, Zou-He density on top
+    sh = (1, 1, 129)
+    den = np.ones(sh); den[:, :, -1] = 0.995
+    out.append(dict(name="edge_column_sym", lat=list(sh), scheme=REG, kvisc=0.05, g=[0, 0, -1e-5],
+                    bc=[SYM, SYM, PER, PER, WALL, FD], phase=np.ones(sh, np.uint8), den=den,
+                    vel=0.005 * rng.standard_normal(sh + (3,)), acc=None, chunks=[9, 8]))
+    # a flat sheet (nz = 1): Zou-He velocity / density on the y faces of a
+    # 2 x 3 x 1 lattice, periodic x and z
+    sh = (2, 3, 1)
+    vel = np.zeros(sh + (3,)); vel[:, 0, :, 1] = 0.02
+    out.append(dict(name="edge_sheet_zou_he", lat=list(sh), scheme=BGK, kvisc=0.1, g=[1e-5, 0, 0],
+                    bc=[PER, PER, FV, FD, PER, PER], phase=np.ones(sh, np.uint8), den=np.ones(sh),
+                    vel=vel, acc=None, chunks=[5, 6]))
+    # one fluid site enclosed by solids, two of which move (Ladd) with a
+    # velocity component along their link to the site
+    sh = (3, 3, 3)
+    ph = np.zeros(sh, np.uint8); ph[1, 1, 1] = 1
+    vel = np.zeros(sh + (3,)); vel[1, 2, 1] = [0.01, 0.01, -0.005]; vel[2, 1, 0] = [0.01, 0.02, -0.01]
+    out.append(dict(name="edge_enclosed_site", lat=list(sh), scheme=TRT, kvisc=0.03, g=[0, 0, 0],
+                    bc=[WALL] * 6, phase=ph, den=np.ones(sh), vel=vel, acc=None, chunks=[6, 7]))
     return out
 
 
@@ -136,8 +165,10 @@ def run(case):
     return nf, decode_bundle_c(s), np.array(s.get_den()), np.array(s.get_vel())
 
 
-def main():
+def main(names=None):
     for case in cases():
+        if names and case["name"] not in names:
+            continue
         nf, f, den, vel = run(case)
         meta = {k: case[k] for k in ("name", "lat", "scheme", "kvisc", "g", "bc", "chunks")}
         meta["nfluid"] = int(nf)
@@ -150,4 +181,5 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    # optional case names: write only those fixtures
+    main(sys.argv[1:])

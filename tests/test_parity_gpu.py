@@ -188,6 +188,24 @@ def test_reduced_precision_velocity_error(name, precision, tol):
     assert abs(den[fl] - c["den"][fl]).max() <= (1e-6 if precision == 1 else 1e-3)
 
 
+EDGE = ["edge_single_site", "edge_column_sym", "edge_sheet_zou_he", "edge_enclosed_site"]
+
+
+@pytest.mark.parametrize("precision,tol", [(1, 1e-4), (2, 5e-2)])
+@pytest.mark.parametrize("name", EDGE)
+def test_reduced_precision_degenerate_shapes(name, precision, tol):
+    # the FP32 / FP16 kernels on 1-site, 1-column, 1-sheet and enclosed
+    # lattices (the last on the fluid-only layout) against the reference's
+    # FP64 outputs; few sites, so the relative L2 bound is looser than above
+    c = load_case(name)
+    nf, f, den, vel = run_engine(c, precision=precision)
+    assert nf == c["nfluid"]
+    fl = c["phase"] != 0
+    err = np.linalg.norm(vel[fl] - c["vel"][fl]) / np.linalg.norm(c["vel"][fl])
+    assert err <= tol, err
+    assert abs(den[fl] - c["den"][fl]).max() <= (1e-6 if precision == 1 else 1e-3)
+
+
 def test_mass_conserved_large_periodic():
     # size-independent property at a larger size: mass and (force-free)
     # momentum of a periodic box stay constant
