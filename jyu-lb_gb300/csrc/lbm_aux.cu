@@ -5,6 +5,8 @@
 //   * moment download straight into mapped host arrays;
 //   * acceleration-field upload;
 //   * FP64 mass / momentum reductions (two passes, deterministic order).
+#include <algorithm>
+
 #include "lbm_aux.h"
 #include "lbm_step.cuh"
 
@@ -406,6 +408,49 @@ __global__ void sparse_tables_kernel(const int64_t *rd, const int64_t *wr, const
     if (e < M) nodec[e] = cidx[node[e]];
 }
 
+// velocities of the solid positions next to fluid (halo-padded host vel,
+// read in place) against their values at the last classification: *flag
+// becomes 1 when any component differs (a NaN counts as a change)
+__global__ void wall_check_kernel(const int64_t *pos, const double *known, int64_t nwall, const double *vel,
+                                  int *flag) {
+    for (int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; w < nwall;
+         w += (int64_t)gridDim.x * blockDim.x) {
+        const double *u = vel + 3 * pos[w];
+        if (u[0] != known[3 * w] || u[1] != known[3 * w + 1] || u[2] != known[3 * w + 2]) *flag = 1;
+    }
+}
+
+// per-call data of the boundary nodes read in place from the halo-padded
+// host den/vel: the node's density (Ladd's term; FP32 storage keeps rho - 1)
+// and the Zou-He (den, vel) of each fixed face it lies on; faces outside
+// refresh_mask keep den = 1, vel = 0
+__global__ void fill_dynamic_kernel(AuxGeom g, int M, const int64_t *sp_node, const uint32_t *sp_info,
+                                    unsigned refresh_mask, int f64, const double *den, const double *vel,
+                                    double *bc, void *dbuf) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= M) return;
+    const int64_t n = sp_node[t];
+    const int64_t syz = (int64_t)g.ny * g.nz;
+    const int i = (int)(n / syz);
+    const int j = (int)((n / g.nz) % g.ny);
+    const int k = (int)(n % g.nz);
+    const int64_t fn = ((int64_t)(i + 1) * g.NJ + (j + 1)) * g.NK + (k + 1);
+    if (f64) ((double *)dbuf)[t] = den[fn];
+    else ((float *)dbuf)[t] = (float)(den[fn] - 1.0);
+    const uint32_t faces = (sp_info[t] >> SP_FACE_SHIFT) & 0x3Fu;
+    int slot = 0;
+    for (int face = 0; face < 6 && faces; ++face) {
+        if (!(faces & (1u << face))) continue;
+        double d = 1.0, u0 = 0.0, u1 = 0.0, u2 = 0.0;
+        if (refresh_mask & (1u << face)) { d = den[fn]; u0 = vel[3 * fn]; u1 = vel[3 * fn + 1]; u2 = vel[3 * fn + 2]; }
+        bc[(size_t)(4 * slot) * M + t] = d;
+        bc[(size_t)(4 * slot + 1) * M + t] = u0;
+        bc[(size_t)(4 * slot + 2) * M + t] = u1;
+        bc[(size_t)(4 * slot + 3) * M + t] = u2;
+        slot = 1;
+    }
+}
+
 // ---------------------------------------------------------------------------
 // host-callable launchers
 // ---------------------------------------------------------------------------
@@ -457,6 +502,21 @@ int aux_sparse_pack(int elem_bytes, void *dense, void *comp, const int32_t *csit
         sparse_pack_kernel<uint32_t><<<b, 256, 0, st>>>((uint32_t *)dense, (uint32_t *)comp, csite, Nc, Np, Npc, to_comp);
     else
         sparse_pack_kernel<uint16_t><<<b, 256, 0, st>>>((uint16_t *)dense, (uint16_t *)comp, csite, Nc, Np, Npc, to_comp);
+    return (int)cudaGetLastError();
+}
+
+int aux_wall_check(const int64_t *pos, const double *known, int64_t nwall, const double *vel, int *flag,
+                   cudaStream_t st) {
+    if (nwall <= 0) return 0;
+    const unsigned b = (unsigned)std::min<int64_t>(nblk(nwall, 256), 4096);
+    wall_check_kernel<<<b, 256, 0, st>>>(pos, known, nwall, vel, flag);
+    return (int)cudaGetLastError();
+}
+
+int aux_fill_dynamic(const AuxGeom &g, int M, const int64_t *sp_node, const uint32_t *sp_info, unsigned refresh_mask,
+                     int f64, const double *den, const double *vel, double *bc, void *dbuf, cudaStream_t st) {
+    if (M <= 0) return 0;
+    fill_dynamic_kernel<<<nblk(M, 128), 128, 0, st>>>(g, M, sp_node, sp_info, refresh_mask, f64, den, vel, bc, dbuf);
     return (int)cudaGetLastError();
 }
 

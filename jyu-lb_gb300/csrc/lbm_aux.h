@@ -29,6 +29,16 @@ int aux_sparse_pack(int elem_bytes, void *dense, void *comp, const int32_t *csit
 // boundary-node element tables (q * Np + n) -> fluid-only (q * Npc + m)
 int aux_sparse_tables(const int64_t *rd, const int64_t *wr, const int64_t *node, int M, const int32_t *cidx,
                       int64_t Np, int64_t Npc, int64_t *rdc, int64_t *wrc, int64_t *nodec, cudaStream_t st);
+// *flag = 1 (device-accessible int) when vel (device-accessible halo-padded
+// host array) differs from known (3 per position) at any of the nwall
+// positions
+int aux_wall_check(const int64_t *pos, const double *known, int64_t nwall, const double *vel, int *flag,
+                   cudaStream_t st);
+// boundary nodes' per-call density and Zou-He data from device-accessible
+// halo-padded host den/vel (faces in refresh_mask are read, the others get
+// den = 1, vel = 0); dbuf: double (f64) or float (rho - 1)
+int aux_fill_dynamic(const AuxGeom &g, int M, const int64_t *sp_node, const uint32_t *sp_info, unsigned refresh_mask,
+                     int f64, const double *den, const double *vel, double *bc, void *dbuf, cudaStream_t st);
 // rows [row0, row0 + nrows) of (i, j) rows only
 int aux_download_rows(int prec, const AuxGeom &g, const uint32_t *nmask, const void *den, const void *ux,
                       const void *uy, const void *uz, double *hden, double *hvel, int64_t row0, int64_t nrows,

@@ -99,6 +99,10 @@ struct jlb_solver {
     std::vector<uint8_t> hcls;       // Np node classes derived from hmask
     std::vector<int64_t> wall_pos;   // solid positions next to fluid (halo-padded index)
     std::vector<double> wall_vel;    // their velocities at the last classification
+    int64_t *d_wall_pos = nullptr;   // device copies of wall_pos / wall_vel for the in-place check
+    double *d_wall_vel = nullptr;
+    bool wall_dev_dirty = true;      // wall_pos / wall_vel changed since their upload
+    int *wall_flag = nullptr;        // mapped host int set by the check kernel
     std::vector<int64_t> sp_node;
     std::vector<uint32_t> sp_info;
     std::vector<int64_t> sp_rd, sp_wr;
@@ -337,6 +341,7 @@ void build_wall_list(jlb_solver *s) {
     s->wall_pos.clear();
     for (int64_t p = 0; p < s->NCNT; ++p)
         if (flag[p]) s->wall_pos.push_back(p);
+    s->wall_dev_dirty = true;
 }
 
 // boundary-node tables from the current wall velocities (vel: halo-padded,
@@ -366,6 +371,7 @@ void build_special(jlb_solver *s, const double *vel) {
     }
     // moving solids: a bounce-back link with a nonzero Ladd projection
     s->wall_vel.resize(3 * s->wall_pos.size());
+    s->wall_dev_dirty = true;
     for (size_t w = 0; w < s->wall_pos.size(); ++w) {
         const int64_t p = s->wall_pos[w];
         const double *u = vel + 3 * p;
@@ -553,6 +559,24 @@ int upload_dynamic(jlb_solver *s, const double *den, const double *vel) {
     if (M == 0) return JLB_OK;
     const size_t bc_bytes = 4 * (size_t)s->bc_slots * M * sizeof(double);
     const size_t den_bytes = (size_t)M * s->csz;
+    const double *dden = (const double *)dev_view(den), *dvel = (const double *)dev_view(vel);
+    if (dden && dvel) {
+        // page-locked host arrays: a kernel reads the face layers in place
+        // (stream-ordered after the previous steps, no host pass, no staging)
+        const int *bc = s->cfg.bc;
+        unsigned refresh = 0;
+        for (int face = 0; face < 6; ++face) {
+            // the reference refreshes face Z1's data when bc[Z1] is FIXED_DEN
+            // or bc[1Z] is FIXED_VEL (jyulb/isothermal.pyx:500)
+            const bool r = face == 5 ? (bc[5] == BC_FIXED_DEN || bc[4] == BC_FIXED_VEL) : is_fixed(bc[face]);
+            if (r) refresh |= 1u << face;
+        }
+        CKR(aux_fill_dynamic(s->geom, M, s->d_sp_node, s->d_sp_info, refresh, s->prec == PREC_FP64, dden, dvel,
+                             s->d_sp_bc, s->d_sp_den, s->st));
+        ++s->launches;
+        s->h2d_bytes += bc_bytes + den_bytes;
+        return JLB_OK;
+    }
     int r = ensure_pinned(s, bc_bytes + den_bytes + 64);
     if (r) return r;
     CK(cudaStreamSynchronize(s->st)); // staging buffer may still be in flight
@@ -809,6 +833,38 @@ int run_steps(jlb_solver *s, uint32_t n, bool write_last) {
     return JLB_OK;
 }
 
+// solid velocities changed since the last classification?  A kernel reads
+// the page-locked host vel in place at the wall positions (the host loop
+// over them is latency-bound: ~1.2 ms single-threaded, ~0.14 ms on 16
+// threads for the 256^3 cavity's 330 K positions)
+int wall_check_device(jlb_solver *s, const double *dvel, int &changed) {
+    const int64_t nwall = (int64_t)s->wall_pos.size();
+    if (!s->wall_flag) {
+        CK(cudaHostAlloc((void **)&s->wall_flag, sizeof(int), cudaHostAllocMapped));
+    }
+    if (s->wall_dev_dirty) {
+        cudaFree(s->d_wall_pos);
+        cudaFree(s->d_wall_vel);
+        s->d_wall_pos = nullptr;
+        s->d_wall_vel = nullptr;
+        CK(cudaMalloc(&s->d_wall_pos, nwall * sizeof(int64_t)));
+        CK(cudaMalloc(&s->d_wall_vel, 3 * nwall * sizeof(double)));
+        CK(cudaMemcpyAsync(s->d_wall_pos, s->wall_pos.data(), nwall * sizeof(int64_t), cudaMemcpyHostToDevice,
+                           s->st));
+        CK(cudaMemcpyAsync(s->d_wall_vel, s->wall_vel.data(), 3 * nwall * sizeof(double), cudaMemcpyHostToDevice,
+                           s->st));
+        s->wall_dev_dirty = false;
+    }
+    int *dflag = nullptr;
+    CK(cudaHostGetDevicePointer((void **)&dflag, s->wall_flag, 0));
+    *(volatile int *)s->wall_flag = 0;
+    CKR(aux_wall_check(s->d_wall_pos, s->d_wall_vel, nwall, dvel, dflag, s->st));
+    ++s->launches;
+    CK(cudaStreamSynchronize(s->st));
+    changed = *(volatile int *)s->wall_flag;
+    return JLB_OK;
+}
+
 // copies planes [i0, i1) of the interior box of a halo-padded host array
 // (comps doubles per site) from its device copy with one pitched 3-D copy
 cudaError_t copy_interior(const jlb_solver *s, const double *src, double *dst, int comps, int i0, int i1,
@@ -928,8 +984,14 @@ int final_step_overlapped(jlb_solver *s, double *den, double *vel) {
         if ((r = direct(sp, (a.M + 127) / 128))) return r;
     }
     const int kb = a.kblocks;
+    // a thin first slab lets the copies start early; the rest split evenly
+    const int first = std::max(1, s->nx / 32);
+    auto bound = [&](int k) -> int {
+        if (k == 0) return 0;
+        return first + (int)((int64_t)(s->nx - first) * (k - 1) / (nslab - 1));
+    };
     for (int k = 0; k < nslab; ++k) {
-        const int i0 = (int)((int64_t)s->nx * k / nslab), i1 = (int)((int64_t)s->nx * (k + 1) / nslab);
+        const int i0 = bound(k), i1 = k + 1 == nslab ? s->nx : bound(k + 1);
         if (i1 <= i0) continue;
         StepArgs sl = a;
         sl.M = 0;
@@ -1093,10 +1155,12 @@ void jlb_destroy(jlb_solver *s) {
     void *bufs[] = {s->f, s->nmask, s->ncls, s->mom[0], s->mom[1], s->mom[2], s->mom[3], s->acc, s->red_partial,
                     s->red_out, s->d_sp_node, s->d_sp_info, s->d_sp_rd, s->d_sp_wr, s->d_sp_lw, s->d_sp_bc,
                     s->d_sp_den, s->d_err, s->fi_partial, s->fi_out, s->stg_den, s->stg_vel,
-                    s->fc, s->d_csite, s->d_cidx, s->d_sp_rd_c, s->d_sp_wr_c, s->d_sp_cnode};
+                    s->fc, s->d_csite, s->d_cidx, s->d_sp_rd_c, s->d_sp_wr_c, s->d_sp_cnode,
+                    s->d_wall_pos, s->d_wall_vel};
     for (void *p : bufs)
         if (p) cudaFree(p);
     if (s->pinned) cudaFreeHost(s->pinned);
+    if (s->wall_flag) cudaFreeHost(s->wall_flag);
     for (cudaEvent_t e : s->slab_ev) cudaEventDestroy(e);
     if (s->st2) { cudaStreamSynchronize(s->st2); cudaStreamDestroy(s->st2); }
     if (s->own_stream && s->st) cudaStreamDestroy(s->st);
@@ -1226,10 +1290,16 @@ int jlb_evolve(jlb_solver *s, uint32_t tsteps, const double g[3], double *den, d
     // solid velocities: reclassify when any of them changed since the last call
     int changed = 0;
     const int64_t nwall = (int64_t)s->wall_pos.size();
+    const double *dvel = (const double *)dev_view(vel);
+    if (nwall > 0 && dvel) {
+        int r = wall_check_device(s, dvel, changed);
+        if (r) return r;
+    } else {
 #pragma omp parallel for schedule(static) reduction(| : changed) if (nwall > 16384)
-    for (int64_t w = 0; w < nwall; ++w) {
-        const double *u = vel + 3 * s->wall_pos[w];
-        changed |= (u[0] != s->wall_vel[3 * w]) | (u[1] != s->wall_vel[3 * w + 1]) | (u[2] != s->wall_vel[3 * w + 2]);
+        for (int64_t w = 0; w < nwall; ++w) {
+            const double *u = vel + 3 * s->wall_pos[w];
+            changed |= (u[0] != s->wall_vel[3 * w]) | (u[1] != s->wall_vel[3 * w + 1]) | (u[2] != s->wall_vel[3 * w + 2]);
+        }
     }
     if (changed) {
         build_special(s, vel);
