@@ -113,6 +113,15 @@ int jlb_finalize_init(jlb_solver *s, uint8_t *phase, double *den, double *vel,
 int jlb_evolve(jlb_solver *s, uint32_t tsteps, const double g[3], double *den,
                double *vel, const double *acc, uint32_t *tot);
 
+/* With on != 0 the caller promises not to write den/vel in the halo cells of
+ * WALL, FIXED_DEN and FIXED_VEL faces after jlb_finalize_init, as with the
+ * reference's Solver, whose getters reach the interior only
+ * (jyulb/isothermal.pyx:1465-1511).  jlb_evolve then re-reads solid
+ * velocities only in the interior and in the halo cells of periodic and
+ * symmetric faces, which its halo rules refresh from the interior.  Off by
+ * default; no reference counterpart. */
+int jlb_set_static_halo(jlb_solver *s, int on);
+
 /* Uploads the per-site field of the halo-padded (NI,NJ,NK,3) array acc
  * (acceleration, or force density with JLB_KERNEL_CXX) now, so that
  * jlb_finalize_init uses it: the C++ executable's initial state includes the

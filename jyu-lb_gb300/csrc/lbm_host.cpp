@@ -99,7 +99,9 @@ struct jlb_solver {
     std::vector<uint8_t> hcls;       // Np node classes derived from hmask
     std::vector<int64_t> wall_pos;   // solid positions next to fluid (halo-padded index)
     std::vector<double> wall_vel;    // their velocities at the last classification
-    int64_t *d_wall_pos = nullptr;   // device copies of wall_pos / wall_vel for the in-place check
+    std::vector<int64_t> wall_chk;   // indices into wall_pos re-read at every evolve call
+    bool static_halo = false;        // halo cells of closed faces are not written by the caller
+    int64_t *d_wall_pos = nullptr;   // device copies of the checked wall_pos / wall_vel
     double *d_wall_vel = nullptr;
     bool wall_dev_dirty = true;      // wall_pos / wall_vel changed since their upload
     int *wall_flag = nullptr;        // mapped host int set by the check kernel
@@ -325,6 +327,46 @@ void build_mask(jlb_solver *s) {
     s->nfluid = cnt;
 }
 
+// halo positions that the halo rules of jlb_evolve rewrite from the
+// interior (periodic and symmetric faces, jyulb/isothermal.pyx:582-686)
+std::vector<uint8_t> halo_refreshed(const jlb_solver *s) {
+    std::vector<uint8_t> m((size_t)s->NCNT, 0);
+    for (int face = 0; face < 6; ++face) {
+        const int b = s->cfg.bc[face];
+        if (b != BC_PERIODIC && b != BC_SYMMETRIC) continue;
+        const int ax = face >> 1;
+        int rd, wr;
+        halo_rw(s, face, rd, wr);
+        face_loop(s, ax, [&](int ua, int ub) {
+            int I, J, K;
+            plane(ax, wr, ua, ub, I, J, K);
+            m[fidx(s, I, J, K)] = 1;
+        });
+    }
+    return m;
+}
+
+// the wall positions whose velocities jlb_evolve re-reads: all of them, or
+// with a static halo all but the halo cells that neither the caller nor the
+// halo rules write (those of wall and Zou-He faces)
+void select_checked_walls(jlb_solver *s) {
+    s->wall_chk.clear();
+    std::vector<uint8_t> refreshed;
+    if (s->static_halo) refreshed = halo_refreshed(s);
+    for (size_t w = 0; w < s->wall_pos.size(); ++w) {
+        const int64_t p = s->wall_pos[w];
+        if (s->static_halo) {
+            const int I = (int)(p / ((int64_t)s->NJ * s->NK));
+            const int J = (int)((p / s->NK) % s->NJ);
+            const int K = (int)(p % s->NK);
+            const bool halo = I == 0 || J == 0 || K == 0 || I == s->NI - 1 || J == s->NJ - 1 || K == s->NK - 1;
+            if (halo && !refreshed[p]) continue;
+        }
+        s->wall_chk.push_back((int64_t)w);
+    }
+    s->wall_dev_dirty = true;
+}
+
 // solid positions that are the source of a bounce-back link
 void build_wall_list(jlb_solver *s) {
     std::vector<uint8_t> flag((size_t)s->NCNT, 0);
@@ -341,7 +383,7 @@ void build_wall_list(jlb_solver *s) {
     s->wall_pos.clear();
     for (int64_t p = 0; p < s->NCNT; ++p)
         if (flag[p]) s->wall_pos.push_back(p);
-    s->wall_dev_dirty = true;
+    select_checked_walls(s);
 }
 
 // boundary-node tables from the current wall velocities (vel: halo-padded,
@@ -838,21 +880,26 @@ int run_steps(jlb_solver *s, uint32_t n, bool write_last) {
 // over them is latency-bound: ~1.2 ms single-threaded, ~0.14 ms on 16
 // threads for the 256^3 cavity's 330 K positions)
 int wall_check_device(jlb_solver *s, const double *dvel, int &changed) {
-    const int64_t nwall = (int64_t)s->wall_pos.size();
+    const int64_t nwall = (int64_t)s->wall_chk.size();
     if (!s->wall_flag) {
         CK(cudaHostAlloc((void **)&s->wall_flag, sizeof(int), cudaHostAllocMapped));
     }
     if (s->wall_dev_dirty) {
+        std::vector<int64_t> pos((size_t)nwall);
+        std::vector<double> known(3 * (size_t)nwall);
+        for (int64_t c = 0; c < nwall; ++c) {
+            const int64_t w = s->wall_chk[c];
+            pos[c] = s->wall_pos[w];
+            for (int d = 0; d < 3; ++d) known[3 * c + d] = s->wall_vel[3 * w + d];
+        }
         cudaFree(s->d_wall_pos);
         cudaFree(s->d_wall_vel);
         s->d_wall_pos = nullptr;
         s->d_wall_vel = nullptr;
         CK(cudaMalloc(&s->d_wall_pos, nwall * sizeof(int64_t)));
         CK(cudaMalloc(&s->d_wall_vel, 3 * nwall * sizeof(double)));
-        CK(cudaMemcpyAsync(s->d_wall_pos, s->wall_pos.data(), nwall * sizeof(int64_t), cudaMemcpyHostToDevice,
-                           s->st));
-        CK(cudaMemcpyAsync(s->d_wall_vel, s->wall_vel.data(), 3 * nwall * sizeof(double), cudaMemcpyHostToDevice,
-                           s->st));
+        CK(cudaMemcpy(s->d_wall_pos, pos.data(), nwall * sizeof(int64_t), cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(s->d_wall_vel, known.data(), 3 * nwall * sizeof(double), cudaMemcpyHostToDevice));
         s->wall_dev_dirty = false;
     }
     int *dflag = nullptr;
@@ -1266,6 +1313,13 @@ int jlb_set_acc(jlb_solver *s, const double *acc) {
     return JLB_OK;
 }
 
+int jlb_set_static_halo(jlb_solver *s, int on) {
+    if (!s) return fail(s, JLB_ERR_INVALID_ARG, "NULL solver");
+    s->static_halo = on != 0;
+    if (s->init_done) select_checked_walls(s);
+    return JLB_OK;
+}
+
 int jlb_evolve(jlb_solver *s, uint32_t tsteps, const double g[3], double *den, double *vel, const double *acc,
                uint32_t *tot) {
     if (!s) return fail(s, JLB_ERR_INVALID_ARG, "NULL solver");
@@ -1289,14 +1343,15 @@ int jlb_evolve(jlb_solver *s, uint32_t tsteps, const double g[3], double *den, d
     enforce_den_vel(s, den, vel);
     // solid velocities: reclassify when any of them changed since the last call
     int changed = 0;
-    const int64_t nwall = (int64_t)s->wall_pos.size();
+    const int64_t nchk = (int64_t)s->wall_chk.size();
     const double *dvel = (const double *)dev_view(vel);
-    if (nwall > 0 && dvel) {
+    if (nchk > 0 && dvel) {
         int r = wall_check_device(s, dvel, changed);
         if (r) return r;
     } else {
-#pragma omp parallel for schedule(static) reduction(| : changed) if (nwall > 16384)
-        for (int64_t w = 0; w < nwall; ++w) {
+#pragma omp parallel for schedule(static) reduction(| : changed) if (nchk > 16384)
+        for (int64_t c = 0; c < nchk; ++c) {
+            const int64_t w = s->wall_chk[c];
             const double *u = vel + 3 * s->wall_pos[w];
             changed |= (u[0] != s->wall_vel[3 * w]) | (u[1] != s->wall_vel[3 * w + 1]) | (u[2] != s->wall_vel[3 * w + 2]);
         }

@@ -22,7 +22,7 @@ JLB_ERR_NUMERIC = -6
 
 # every symbol include/jyulb_gb300.h declares
 EXPORTED_SYMBOLS = (
-    "jlb_check_config", "jlb_create", "jlb_destroy", "jlb_finalize_init", "jlb_set_acc", "jlb_evolve",
+    "jlb_check_config", "jlb_create", "jlb_destroy", "jlb_finalize_init", "jlb_set_acc", "jlb_set_static_halo", "jlb_evolve",
     "jlb_step", "jlb_download_moments", "jlb_get_populations", "jlb_set_populations",
     "jlb_reduce", "jlb_flow_info", "jlb_reduce_moments_noalloc", "jlb_tot_tsteps", "jlb_rlx_prm", "jlb_kernel_launches",
     "jlb_transfer_bytes", "jlb_host_timers",
@@ -92,6 +92,7 @@ def load() -> ctypes.CDLL:
         "jlb_destroy": (None, [vp]),
         "jlb_finalize_init": (ctypes.c_int, [vp, u8p, dp, dp, ctypes.POINTER(ctypes.c_uint64)]),
         "jlb_set_acc": (ctypes.c_int, [vp, dp]),
+        "jlb_set_static_halo": (ctypes.c_int, [vp, ctypes.c_int]),
         "jlb_evolve": (ctypes.c_int, [vp, ctypes.c_uint32, dp, dp, dp, dp, ctypes.POINTER(ctypes.c_uint32)]),
         "jlb_step": (ctypes.c_int, [vp, ctypes.c_uint32, ctypes.c_int]),
         "jlb_download_moments": (ctypes.c_int, [vp, dp, dp]),

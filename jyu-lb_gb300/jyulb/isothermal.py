@@ -19,7 +19,9 @@ writes them in place.  As in the reference:
   ``den``/``vel`` of the Zou-He face layers are the boundary data; both are
   re-read at every ``evolve`` call;
 * ``acc`` is added to gravity at every step (read at every ``evolve`` call
-  once a view of it has been handed out).
+  once a view of it has been handed out);
+* the halo cells of wall and Zou-He faces, which the reference's getters do
+  not reach, keep the values they had at ``finalize_init``.
 
 Additions of this engine (keyword-only): ``precision`` (defs.FP64 / FP32 /
 FP16), ``trt_magic`` (TRT magic parameter; None keeps the reference's 3/16) and
@@ -183,6 +185,10 @@ class Solver:
             raise _native.EngineUnavailable(f'CUDA engine unavailable: {msg}')
         self._lib = lib
         self._h = h
+        # the getters reach the interior only, as the reference's do, so the
+        # halo cells of wall and Zou-He faces keep their initial values and
+        # evolve need not re-read their solid velocities
+        lib.jlb_set_static_halo(h, 1)
 
     def __del__(self):
         h = getattr(self, '_h', None)

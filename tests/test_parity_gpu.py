@@ -116,6 +116,57 @@ def test_moving_walls_change_between_calls():
     np.testing.assert_array_equal(np.asarray(s.get_vel())[fl], o.get_vel()[fl])
 
 
+def _walls_case(bc, seed):
+    from pyoracle import Oracle
+
+    c = _random_case(seed, (7, 6, 8), 1, bc, porosity=0.8, moving=False, acc=False, chunks=(4,))
+    o = Oracle(c["lat"], c["scheme"], c["kvisc"], c["g"], c["bc"])
+    s = make_engine(c)
+    for obj in (o, s):
+        obj.get_phase()[:] = c["phase"]
+        obj.get_den()[:] = c["den0"]
+        obj.get_vel()[:] = c["vel0"]
+    assert s.finalize_init() == o.finalize_init()
+    return c, o, s
+
+
+def test_moving_walls_mixed_faces_static_halo():
+    # the Solver's default: halo cells of wall faces are not re-read; interior
+    # solids (and their periodic / symmetric halo images) are
+    c, o, s = _walls_case([1, 1, 0, 0, 4, 4], 21)
+    sol = c["phase"] == 0
+    rng = np.random.default_rng(8)
+    for it in range(3):
+        for obj in (o, s):
+            obj.evolve(3 + it)
+        w = 0.01 * rng.standard_normal((int(sol.sum()), 3))
+        for obj in (o, s):
+            obj.get_vel()[sol] = w
+    for obj in (o, s):
+        obj.evolve(4)
+    fl = ~sol
+    np.testing.assert_array_equal(s.populations()[:, fl], o.populations()[:, fl])
+    np.testing.assert_array_equal(np.asarray(s.get_vel())[fl], o.get_vel()[fl])
+
+
+def test_halo_wall_velocity_reread_without_static_halo():
+    # through the C ABI default (no static-halo promise) a velocity written
+    # into the halo of a wall face moves that wall, as in the reference's
+    # stream step, which reads the halo solid's velocity (Ladd)
+    c, o, s = _walls_case([0, 0, 1, 1, 1, 1], 22)
+    assert s._lib.jlb_set_static_halo(s._h, 0) == 0
+    for obj in (o, s):
+        obj.evolve(3)
+    for obj in (o, s):
+        obj.vel[0, 1:-1, 1:-1, 1] = 0.02
+        obj.vel[-1, 1:-1, 1:-1, 2] = -0.01
+    for obj in (o, s):
+        obj.evolve(5)
+    fl = c["phase"] != 0
+    np.testing.assert_array_equal(s.populations()[:, fl], o.populations()[:, fl])
+    np.testing.assert_array_equal(np.asarray(s.get_vel())[fl], o.get_vel()[fl])
+
+
 def test_acc_and_gravity_updates_between_calls():
     from pyoracle import Oracle
 
