@@ -310,7 +310,8 @@ def run_ensemble(args):
     # total step count
     errs = []
     total = args.warmup + args.steps
-    for d in range(0, len(doms), max(1, len(doms) // args.check_domains))[: args.check_domains]:
+    sample = range(0, len(doms), max(1, len(doms) // max(1, args.check_domains)))[: args.check_domains]
+    for d in sample:
         dom = doms[d]
         s = Solver(np.array(dom.phase.shape, dtype=np.int32), BGK, dom.kvisc, dom.g, None, precision=FP64)
         s.get_phase()[:] = dom.phase
