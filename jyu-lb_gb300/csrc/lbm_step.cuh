@@ -387,6 +387,9 @@ __device__ __forceinline__ void sparse_node(const StepArgs &a, int b) {
 #ifndef JLB_MIN_BLOCKS_SPARSE
 #define JLB_MIN_BLOCKS_SPARSE JLB_MIN_BLOCKS
 #endif
+#ifndef JLB_MIN_BLOCKS_SPARSE_L
+#define JLB_MIN_BLOCKS_SPARSE_L JLB_MIN_BLOCKS_SPARSE
+#endif
 template <class ST, class PH, bool PSTEP, bool ACCF, class IT>
 __global__ void __launch_bounds__(128, JLB_MIN_BLOCKS_STEP) lbm_step_kernel(const StepArgs a) {
     const int b = (int)blockIdx.x;
@@ -395,7 +398,8 @@ __global__ void __launch_bounds__(128, JLB_MIN_BLOCKS_STEP) lbm_step_kernel(cons
 }
 
 template <class ST, class PH, bool PSTEP, bool ACCF>
-__global__ void __launch_bounds__(128, JLB_MIN_BLOCKS_SPARSE) lbm_step_sparse_kernel(const StepArgs a) {
+__global__ void __launch_bounds__(128, PSTEP ? JLB_MIN_BLOCKS_SPARSE : JLB_MIN_BLOCKS_SPARSE_L)
+    lbm_step_sparse_kernel(const StepArgs a) {
     const int b = (int)blockIdx.x;
     const int nbc = (int)((a.Nc + 127) / 128);
     if (b < nbc) sparse_node<ST, PH, PSTEP, ACCF>(a, b);
