@@ -32,7 +32,10 @@ __device__ __forceinline__ int32_t split_div(int32_t l, int32_t d, float inv, in
 #ifndef JLB_BATCH_WARPS
 #define JLB_BATCH_WARPS 32
 #endif
-template <int SCH, bool PSTEP, int BLOCK>
+// IDX32: every element index q * Np + n fits 32 unsigned bits (19 Np < 2^32),
+// so an address is one select of two 32-bit indices and one widening
+// multiply-add; otherwise each population row has its own 64-bit pointer
+template <int SCH, bool PSTEP, int BLOCK, bool IDX32>
 __global__ void __launch_bounds__(BLOCK, JLB_BATCH_WARPS * 32 / BLOCK)
     lbm_batch_kernel(const BatchArgs a) {
     using ST = StoreF32;
@@ -65,13 +68,25 @@ __global__ void __launch_bounds__(BLOCK, JLB_BATCH_WARPS * 32 / BLOCK)
         dJ[0] = (j == 0 ? (ny - 1) : -1) * nz; dJ[1] = 0; dJ[2] = (j + 1 == ny ? (1 - ny) : 1) * nz;
         dK[0] = k == 0 ? (nz - 1) : -1; dK[1] = 0; dK[2] = k + 1 == nz ? (1 - nz) : 1;
     }
+    const uint32_t Npu = (uint32_t)a.Np;
     Unroll<0, Q>::run([&]<int q>() {
         const float *p;
-        if (!PSTEP || q == 9) {
-            p = a.fq[q] + n;
+        if constexpr (IDX32) {
+            uint32_t e;
+            if (!PSTEP || q == 9) {
+                e = (uint32_t)q * Npu + (uint32_t)n;
+            } else {
+                const int32_t src = n + dI[1 - CX(q)] + dJ[1 - CY(q)] + dK[1 - CZ(q)];
+                e = (m & (1u << q)) ? (uint32_t)q * Npu + (uint32_t)n : (uint32_t)OPP(q) * Npu + (uint32_t)src;
+            }
+            p = a.f + e;
         } else {
-            const int32_t src = n + dI[1 - CX(q)] + dJ[1 - CY(q)] + dK[1 - CZ(q)];
-            p = (m & (1u << q)) ? (a.fq[q] + n) : (a.fq[OPP(q)] + src);
+            if (!PSTEP || q == 9) {
+                p = a.fq[q] + n;
+            } else {
+                const int32_t src = n + dI[1 - CX(q)] + dJ[1 - CY(q)] + dK[1 - CZ(q)];
+                p = (m & (1u << q)) ? (a.fq[q] + n) : (a.fq[OPP(q)] + src);
+            }
         }
         fv[q] = ST::template ld<q>(p);
     });
@@ -88,16 +103,25 @@ __global__ void __launch_bounds__(BLOCK, JLB_BATCH_WARPS * 32 / BLOCK)
     C ux, uy, uz;
     const C dd = PH::collide(fv, D.g[0], D.g[1], D.g[2], D.we, D.wo, ux, uy, uz);
     Unroll<0, Q>::run([&]<int q>() {
-        if (!PSTEP) {
-            ST::template st<OPP(q)>(a.fq[OPP(q)] + n, fv[q]);
-            return;
-        }
         float *p;
-        if (q == 9) {
-            p = a.fq[9] + n;
+        if constexpr (IDX32) {
+            uint32_t e;
+            if (!PSTEP || q == 9) {
+                e = (uint32_t)OPP(q) * Npu + (uint32_t)n;
+            } else {
+                const int32_t dst = n + dI[1 + CX(q)] + dJ[1 + CY(q)] + dK[1 + CZ(q)];
+                e = (m & (1u << OPP(q))) ? (uint32_t)OPP(q) * Npu + (uint32_t)n : (uint32_t)q * Npu + (uint32_t)dst;
+            }
+            p = a.f + e;
         } else {
-            const int32_t dst = n + dI[1 + CX(q)] + dJ[1 + CY(q)] + dK[1 + CZ(q)];
-            p = (m & (1u << OPP(q))) ? (a.fq[OPP(q)] + n) : (a.fq[q] + dst);
+            if (!PSTEP) {
+                p = a.fq[OPP(q)] + n;
+            } else if (q == 9) {
+                p = a.fq[9] + n;
+            } else {
+                const int32_t dst = n + dI[1 + CX(q)] + dJ[1 + CY(q)] + dK[1 + CZ(q)];
+                p = (m & (1u << OPP(q))) ? (a.fq[OPP(q)] + n) : (a.fq[q] + dst);
+            }
         }
         ST::template st<q>(p, fv[q]);
     });
@@ -111,7 +135,10 @@ __global__ void __launch_bounds__(BLOCK, JLB_BATCH_WARPS * 32 / BLOCK)
 }
 
 int launch_batch_step(const BatchArgs &a, int scheme, bool pstep, int block, int ntiles, cudaStream_t st) {
-#define JLB_B(SCH, P, B) lbm_batch_kernel<SCH, P, B><<<ntiles, B, 0, st>>>(a)
+    const bool idx32 = 19 * a.Np < (int64_t(1) << 32);
+#define JLB_B(SCH, P, B)                                                                 \
+    if (idx32) lbm_batch_kernel<SCH, P, B, true><<<ntiles, B, 0, st>>>(a);               \
+    else lbm_batch_kernel<SCH, P, B, false><<<ntiles, B, 0, st>>>(a)
 #define JLB_BB(SCH, B) if (pstep) JLB_B(SCH, true, B); else JLB_B(SCH, false, B);
 #define JLB_BS(SCH)                               \
     if (block == 64) { JLB_BB(SCH, 64) }          \
