@@ -705,8 +705,10 @@ void choose_kernel(jlb_solver *s) {
     // are partly solid slots (1.6x the fluid bytes at porosity 0.6).
     // JLB_SPARSE=0 keeps the lattice layout, JLB_SPARSE=1 forces the other.
     const char *es = std::getenv("JLB_SPARSE");
+    // (32-bit element indices: 19 * Npc < 2^32)
+    const int64_t npc = (((int64_t)s->nfluid + 127) / 128) * 128;
     s->sparse = !s->no_sparse && s->prec != PREC_FP64 && s->cfg.kernel == JLB_KERNEL_JYULB &&
-                s->N < (int64_t)1 << 31 &&
+                s->N < (int64_t)1 << 31 && 19 * npc < ((int64_t)1 << 32) &&
                 ((es && es[0]) ? es[0] == '1' : (double)s->nfluid < 0.8 * (double)s->N);
     s->c_current = false;
     if (s->sparse) { ++s->args_version; return; }

@@ -308,20 +308,21 @@ __device__ __forceinline__ void special_node(const StepArgs &a, int b) {
 // populations of fluid sites are packed (f[q * Npc + m]) and a neighbour's
 // slot is found through the lattice-to-fluid index map (cidx, 4 bytes per
 // lattice site, cached), so only fluid populations move.  Same arithmetic and
-// AA pattern as dense_node.
+// AA pattern as dense_node.  Element indices are 32-bit unsigned: the host
+// uses this layout only when 19 * Npc < 2^32.
 // ---------------------------------------------------------------------------
 template <class ST, class PH, bool PSTEP, bool ACCF>
 __device__ __forceinline__ void sparse_node(const StepArgs &a, int b) {
     using S = typename ST::S;
     using C = typename ST::C;
-    const int64_t m = (int64_t)b * (blockDim.x * blockDim.y) + (threadIdx.y * blockDim.x + threadIdx.x);
-    if (m >= a.Nc) return;
+    const uint32_t m = (uint32_t)b * (blockDim.x * blockDim.y) + (threadIdx.y * blockDim.x + threadIdx.x);
+    if (m >= (uint64_t)a.Nc) return;
     const int32_t n = __ldg(a.csite + m);
     const uint8_t cls = __ldg(a.ncls + n);
     if (cls >= CLS_SPECIAL) return;
     const uint32_t mk = (PSTEP && cls == CLS_WALL) ? __ldg(a.nmask + n) : 0u;
     S *__restrict__ f = (S *)a.f;
-    const int64_t Npc = a.Npc;
+    const uint32_t Npc = (uint32_t)a.Npc; // 19 * Npc < 2^32 (checked by the host)
     int32_t dI[3], dJ[3], dK[3];
     if (PSTEP) {
         const int32_t syz = a.ny * a.nz;
@@ -332,15 +333,15 @@ __device__ __forceinline__ void sparse_node(const StepArgs &a, int b) {
     }
     // fluid index of the neighbour across link q (site x + c_q); only asked
     // for links that do not bounce back, whose neighbour is fluid
-    auto nbr = [&]<int q>() -> int64_t {
-        return __ldg(a.cidx + (n + dI[1 + CX(q)] + dJ[1 + CY(q)] + dK[1 + CZ(q)]));
+    auto nbr = [&]<int q>() -> uint32_t {
+        return (uint32_t)__ldg(a.cidx + (n + dI[1 + CX(q)] + dJ[1 + CY(q)] + dK[1 + CZ(q)]));
     };
     C fv[Q];
     Unroll<0, Q>::run([&]<int q>() {
-        int64_t e;
-        if (!PSTEP || q == 9) e = (int64_t)q * Npc + m;
-        else if (mk & (1u << q)) e = (int64_t)q * Npc + m;
-        else e = (int64_t)OPP(q) * Npc + nbr.template operator()<OPP(q)>();
+        uint32_t e;
+        if (!PSTEP || q == 9) e = (uint32_t)q * Npc + m;
+        else if (mk & (1u << q)) e = (uint32_t)q * Npc + m;
+        else e = (uint32_t)OPP(q) * Npc + nbr.template operator()<OPP(q)>();
         fv[q] = ST::template ld<q>(f + e);
     });
     C ux, uy, uz;
@@ -356,13 +357,13 @@ __device__ __forceinline__ void sparse_node(const StepArgs &a, int b) {
     const C rho = PH::collide(fv, ax, ay, az, (C)a.w_e, (C)a.w_o, ux, uy, uz);
     Unroll<0, Q>::run([&]<int q>() {
         if (!PSTEP) {
-            ST::template st<OPP(q)>(f + ((int64_t)OPP(q) * Npc + m), fv[q]);
+            ST::template st<OPP(q)>(f + ((uint32_t)OPP(q) * Npc + m), fv[q]);
             return;
         }
-        int64_t e;
-        if (q == 9) e = 9 * Npc + m;
-        else if (mk & (1u << OPP(q))) e = (int64_t)OPP(q) * Npc + m;
-        else e = (int64_t)q * Npc + nbr.template operator()<q>();
+        uint32_t e;
+        if (q == 9) e = 9u * Npc + m;
+        else if (mk & (1u << OPP(q))) e = (uint32_t)OPP(q) * Npc + m;
+        else e = (uint32_t)q * Npc + nbr.template operator()<q>();
         ST::template st<q>(f + e, fv[q]);
     });
     if (a.write_moments) {
