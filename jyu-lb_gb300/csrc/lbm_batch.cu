@@ -15,17 +15,6 @@
 
 namespace jlb {
 
-// floor(l / d) and the remainder for 0 <= l < 2^23, from a float reciprocal:
-// the product is within 1 of l/d, so one correction step either way is exact
-__device__ __forceinline__ int32_t split_div(int32_t l, int32_t d, float inv, int32_t &rem) {
-    int32_t q = (int32_t)((float)l * inv);
-    int32_t r = l - q * d;
-    if (r < 0) { --q; r += d; }
-    else if (r >= d) { ++q; r -= d; }
-    rem = r;
-    return q;
-}
-
 // resident warps per SM asked of the register allocator: the P step is
 // latency-bound, and 32 warps beat 24 on the 512-channel ensemble although
 // the P step then spills a few registers

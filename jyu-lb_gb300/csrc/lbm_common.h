@@ -65,6 +65,7 @@ struct StepArgs {
     const int32_t *csite; // [Nc] lattice site n of fluid site m
     const int32_t *cidx;  // [N] fluid index m of lattice site n (-1: solid)
     int64_t Nc, Npc;      // fluid sites, their slot stride (multiple of 128)
+    float inv_syz, inv_nz; // 1/(ny*nz), 1/nz for the site -> (i,j,k) split; 0: use integer division
     const int64_t *sp_cnode; // [M] fluid index of each boundary node (sparse layout), else NULL
     // boundary (special) nodes
     int M;                // number of boundary nodes

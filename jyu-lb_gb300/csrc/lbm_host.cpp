@@ -660,6 +660,12 @@ StepArgs make_args(const jlb_solver *s, int write_moments) {
         a.cidx = s->d_cidx;
         a.Nc = s->Nc;
         a.Npc = s->Npc;
+        // float-reciprocal split when every quotient (i < nx, j < ny) stays
+        // below 2^21 and the divisors below 2^30
+        if (s->nx < (1 << 21) && s->ny < (1 << 21) && (int64_t)s->ny * s->nz < (1 << 30)) {
+            a.inv_syz = 1.0f / (float)((int64_t)s->ny * s->nz);
+            a.inv_nz = 1.0f / (float)s->nz;
+        }
         a.sp_rd = s->d_sp_rd_c;
         a.sp_wr = s->d_sp_wr_c;
         a.sp_cnode = s->d_sp_cnode;

@@ -110,6 +110,19 @@ template <int N> struct Unroll<N, N> {
     template <class F> __device__ __forceinline__ static void run(F &&) {}
 };
 
+// floor(l / d) and the remainder from a float reciprocal inv = 1/d, for
+// 0 <= l < 2^31, 0 < d < 2^30 and a quotient below 2^21: the three roundings
+// (l, inv, product) keep the estimate within 1 of l/d, so one correction
+// step either way is exact (the trial remainder lies in (-d, 2d))
+__device__ __forceinline__ int32_t split_div(int32_t l, int32_t d, float inv, int32_t &rem) {
+    int32_t q = (int32_t)((float)l * inv);
+    int32_t r = (int32_t)((uint32_t)l - (uint32_t)q * (uint32_t)d);
+    if (r < 0) { --q; r += d; }
+    else if (r >= d) { ++q; r -= d; }
+    rem = r;
+    return q;
+}
+
 // ---------------------------------------------------------------------------
 // dense (interior / plain bounce-back / periodic) nodes
 // ---------------------------------------------------------------------------
@@ -326,7 +339,13 @@ __device__ __forceinline__ void sparse_node(const StepArgs &a, int b) {
     int32_t dI[3], dJ[3], dK[3];
     if (PSTEP) {
         const int32_t syz = a.ny * a.nz;
-        const int32_t i = n / syz, r = n - i * syz, j = r / a.nz, k = r - j * a.nz;
+        int32_t i, r, j, k;
+        if (a.inv_syz != 0.0f) {
+            i = split_div(n, syz, a.inv_syz, r);
+            j = split_div(r, a.nz, a.inv_nz, k);
+        } else {
+            i = n / syz; r = n - i * syz; j = r / a.nz; k = r - j * a.nz;
+        }
         dI[0] = (i == 0 ? (a.nx - 1) : -1) * syz; dI[1] = 0; dI[2] = (i + 1 == a.nx ? (1 - a.nx) : 1) * syz;
         dJ[0] = (j == 0 ? (a.ny - 1) : -1) * a.nz; dJ[1] = 0; dJ[2] = (j + 1 == a.ny ? (1 - a.ny) : 1) * a.nz;
         dK[0] = k == 0 ? (a.nz - 1) : -1; dK[1] = 0; dK[2] = k + 1 == a.nz ? (1 - a.nz) : 1;
