@@ -28,11 +28,10 @@ UNITS = {
     # than 6 or 7, even where a few registers spill.  The persistent staged L
     # step keeps its loads in flight as bulk copies and runs fastest at 5
     # blocks for FP32 and 8 for FP16 (sweeps of 4..9 on the 256^3 cavity).
-    # On the fluid-only layout (porous lattices) the P step is fastest at 9
-    # and the L step at 7.
-    "lbm_fp32.cu": ["-DJLB_MIN_BLOCKS=8", "-DJLB_MIN_BLOCKS_TMA=5", "-DJLB_MIN_BLOCKS_SPARSE=9",
-                    "-DJLB_MIN_BLOCKS_SPARSE_L=7"],
-    "lbm_fp16.cu": ["-DJLB_MIN_BLOCKS=8", "-DJLB_MIN_BLOCKS_SPARSE=9", "-DJLB_MIN_BLOCKS_SPARSE_L=7"],
+    # On the fluid-only layout (porous lattices) both steps are fastest at 7
+    # (the P step holds its 18 neighbour indices in registers).
+    "lbm_fp32.cu": ["-DJLB_MIN_BLOCKS=8", "-DJLB_MIN_BLOCKS_TMA=5", "-DJLB_MIN_BLOCKS_SPARSE=7"],
+    "lbm_fp16.cu": ["-DJLB_MIN_BLOCKS=8", "-DJLB_MIN_BLOCKS_SPARSE=7"],
     "lbm_aux.cu": ["-fmad=false"],
     "lbm_noalloc.cu": [],
     "lbm_batch.cu": [],

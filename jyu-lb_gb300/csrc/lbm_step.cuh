@@ -352,9 +352,15 @@ __device__ __forceinline__ void sparse_node(const StepArgs &a, int b) {
     }
     // fluid index of the neighbour across link q (site x + c_q); only asked
     // for links that do not bounce back, whose neighbour is fluid
-    auto nbr = [&]<int q>() -> uint32_t {
-        return (uint32_t)__ldg(a.cidx + (n + dI[1 + CX(q)] + dJ[1 + CY(q)] + dK[1 + CZ(q)]));
-    };
+    // the fluid indices of the 18 neighbours, looked up once for the gather
+    // and the scatter (links that bounce back do not use theirs)
+    uint32_t nb[Q];
+    if (PSTEP) {
+        Unroll<0, Q>::run([&]<int q>() {
+            if (q != 9) nb[q] = (uint32_t)__ldg(a.cidx + (n + dI[1 + CX(q)] + dJ[1 + CY(q)] + dK[1 + CZ(q)]));
+        });
+    }
+    auto nbr = [&]<int q>() -> uint32_t { return nb[q]; };
     C fv[Q];
     Unroll<0, Q>::run([&]<int q>() {
         uint32_t e;
