@@ -61,9 +61,11 @@ def cavity(n, precision, stream=None):
 
 
 class ClockSampler:
-    """nvidia-smi samples of SM clocks and throttle reasons during a region."""
+    """nvidia-smi samples (every 20 ms) of SM clocks and throttle reasons
+    during a region; summary(window) keeps the samples taken inside a
+    wall-clock window (the timed steps), when there are any."""
 
-    FIELDS = ("clocks.sm,clocks.max.sm,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+    FIELDS = ("timestamp,clocks.sm,clocks.max.sm,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
               "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
               "clocks_event_reasons.sw_power_cap")
 
@@ -80,7 +82,7 @@ class ClockSampler:
             self.fh = open(self.out, "w")
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
-                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.fh, stderr=subprocess.DEVNULL)
+                 "--format=csv,noheader,nounits", "-lms", "20"], stdout=self.fh, stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
         time.sleep(0.3)
@@ -95,26 +97,35 @@ class ClockSampler:
                 self.proc.kill()
             self.fh.close()
 
-    def summary(self):
+    def summary(self, window=None):
         if self.proc is None or not os.path.exists(self.out):
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
-        sm, mx, reasons = [], [], set()
+        import datetime
+
+        rows = []
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for line in open(self.out):
             parts = [p.strip() for p in line.split(",")]
-            if len(parts) < 7:
+            if len(parts) < 8:
                 continue
             try:
-                sm.append(float(parts[0]))
-                mx.append(float(parts[1]))
+                ts = datetime.datetime.strptime(parts[0], "%Y/%m/%d %H:%M:%S.%f").timestamp()
+            except ValueError:
+                ts = None  # unknown timestamp format: the sample is kept, unplaced
+            try:
+                rows.append((ts, float(parts[1]), float(parts[2]),
+                             [nm for nm, v in zip(names, parts[4:8]) if v.lower().startswith("active")]))
             except ValueError:
                 continue
-            for nm, v in zip(names, parts[3:7]):
-                if v.lower().startswith("active"):
-                    reasons.add(nm)
         os.remove(self.out)
-        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "samples": len(sm), "reasons": sorted(reasons)}
+        inside = [r for r in rows if window and r[0] is not None and window[0] <= r[0] <= window[1]]
+        sel = inside or rows
+        reasons = sorted({nm for r in sel for nm in r[3]})
+        out = {"sm_mhz": statistics.median(r[1] for r in sel) if sel else None,
+               "sm_max_mhz": max(r[2] for r in sel) if sel else None, "samples": len(sel), "reasons": reasons}
+        if window:
+            out["samples_in_timed_region"] = len(inside)
+        return out
 
 
 def measured_peak():
@@ -142,10 +153,12 @@ def time_device(s, nf, steps, warmup, torch, st):
     torch.cuda.synchronize()
     l0 = s.kernel_launches
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    w0 = time.time()
     e0.record(st)
     assert lib.jlb_step(h, steps, 0) == 0
     e1.record(st)
     torch.cuda.synchronize()
+    time_device.window = (w0, time.time())
     ms = e0.elapsed_time(e1)
     launches = s.kernel_launches - l0
     return nf * steps / (ms * 1e-3) / 1e6, ms / steps, launches
@@ -678,11 +691,12 @@ def main():
     torch.cuda.synchronize()
     with ClockSampler(local) as clk:
         mlups, ms_launch, launches = time_device(s32, nf, args.steps, args.warmup, torch, tstream)
+    win32 = time_device.window
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
     ms_launch, mlups = over_ranks(ms_launch, nf, world, dist, "cuda")
-    clocks = clk.summary()
+    clocks = clk.summary(win32)
     e2e_mlups, e2e_ms, h2d, d2h = 0, 0, 0, 0
     if args.e2e_steps > 0:
         if dist:
@@ -694,11 +708,13 @@ def main():
     s64, _ = cavity(n, FP64, stream)
     with ClockSampler(local) as clk64:
         mlups64, ms64, _ = time_device(s64, nf, max(args.steps // 4, 20), args.warmup, torch, tstream)
+    win64 = time_device.window
     del s64
     torch.cuda.empty_cache()
     s16, _ = cavity(n, FP16, stream)
     with ClockSampler(local) as clk16:
         mlups16, ms16, _ = time_device(s16, nf, args.steps, args.warmup, torch, tstream)
+    win16 = time_device.window
     del s16
     torch.cuda.empty_cache()
     err, err16 = l2_error(n, args.err_steps, stream) if args.err_steps > 0 else (None, None)
@@ -728,11 +744,11 @@ def main():
         "fp64": {"value": round(mlups64, 3), "unit": "MLUPS", "ms_per_step": round(ms64, 5),
                  "roofline_frac": round(ach64 / peak, 4), "achieved_gbs": round(ach64, 1),
                  "bytes_per_site": BYTES_FP64, "fp32_over_fp64": round(mlups / mlups64, 3),
-                 "clocks": clk64.summary()},
+                 "clocks": clk64.summary(win64)},
         "fp16": {"value": round(mlups16, 3), "unit": "MLUPS", "ms_per_step": round(ms16, 5),
                  "roofline_frac": round(nf * 76 / (ms16 * 1e-3) / 1e9 / peak, 4),
                  "achieved_gbs": round(nf * 76 / (ms16 * 1e-3) / 1e9, 1), "bytes_per_site": 76,
-                 "clocks": clk16.summary()},
+                 "clocks": clk16.summary(win16)},
         "error": {"vel_rel_l2_fp32_vs_fp64": err, "vel_rel_l2_fp16_vs_fp64": err16, "steps": args.err_steps},
         "e2e": {"value": round(e2e_mlups, 3), "unit": "MLUPS", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": round(e2e_ms, 4),
