@@ -749,11 +749,8 @@ int check_kernel_error(jlb_solver *s) {
 
 // JLB_OVERLAP_DOWNLOAD=0 keeps the last step and the download in sequence
 bool overlap_off() {
-    static const bool off = [] {
-        const char *e = std::getenv("JLB_OVERLAP_DOWNLOAD");
-        return e && e[0] == '0';
-    }();
-    return off;
+    const char *e = std::getenv("JLB_OVERLAP_DOWNLOAD");
+    return e && e[0] == '0';
 }
 
 bool graphs_enabled() {
@@ -941,10 +938,8 @@ cudaError_t copy_interior(const jlb_solver *s, const double *src, double *dst, i
 // copy of the host layout (allocated on first use).  JLB_DMA_DOWNLOAD=0
 // keeps the kernel path.
 bool dma_ready(jlb_solver *s, double *den, double *vel) {
-    static const bool dma_off = [] {
-        const char *e = std::getenv("JLB_DMA_DOWNLOAD");
-        return e && e[0] == '0';
-    }();
+    const char *de = std::getenv("JLB_DMA_DOWNLOAD");
+    const bool dma_off = de && de[0] == '0';
     if (dma_off || s->stg_failed || s->nfluid != (uint64_t)s->N || !dev_view(den) || !dev_view(vel)) return false;
     if (!s->stg_den) {
         const size_t nb = (size_t)s->NCNT * sizeof(double);
