@@ -238,4 +238,112 @@ template <int SCH> struct PhysSh : PhysShBase {
     }
 };
 
+// The same physics on the stored FP16 values h_q = 2^12 (f_q - w_q) / w_q
+// (StoreF16), used for the bulk of the sites: g_q = w_q 2^-12 h_q enters the
+// moments as weighted class sums, relaxation pairs q with opp(q) of equal
+// weight, and the projection P(H)_q = w_q poly_q(H) adds poly_q(2^12 H) to
+// h_q, so the per-population scale of decode and encode disappears.
+template <int SCH> struct PhysH16 : PhysSh<SCH> {
+    using C = float;
+    static constexpr bool h_space = true;
+
+    __device__ static void project_h(C H0, C hx, C hy, C hz, C hxx, C hxy, C hxz, C hyy, C hyz, C hzz, C *h) {
+        constexpr C K = 4096.0f;
+        H0 *= K; hx *= K; hy *= K; hz *= K;
+        hxx *= K; hxy *= K; hxz *= K; hyy *= K; hyz *= K; hzz *= K;
+        const C tr = hxx + hyy + hzz;
+        const C A0 = fmaf(-1.5f, tr, H0);
+        h[9] += A0;
+        C e, o;
+        e = fmaf(4.5f, hxx, A0); o = 3.0f * hx; h[16] += e + o; h[2] += e - o;
+        e = fmaf(4.5f, hyy, A0); o = 3.0f * hy; h[12] += e + o; h[6] += e - o;
+        e = fmaf(4.5f, hzz, A0); o = 3.0f * hz; h[10] += e + o; h[8] += e - o;
+        const C bxy = fmaf(4.5f, hxx + hyy, A0), bxz = fmaf(4.5f, hxx + hzz, A0), byz = fmaf(4.5f, hyy + hzz, A0);
+        e = fmaf(9.0f, hxy, bxy); o = 3.0f * (hx + hy); h[18] += e + o; h[0] += e - o;
+        e = fmaf(-9.0f, hxy, bxy); o = 3.0f * (hx - hy); h[14] += e + o; h[4] += e - o;
+        e = fmaf(9.0f, hxz, bxz); o = 3.0f * (hx + hz); h[17] += e + o; h[1] += e - o;
+        e = fmaf(-9.0f, hxz, bxz); o = 3.0f * (hx - hz); h[15] += e + o; h[3] += e - o;
+        e = fmaf(9.0f, hyz, byz); o = 3.0f * (hy + hz); h[13] += e + o; h[5] += e - o;
+        e = fmaf(-9.0f, hyz, byz); o = 3.0f * (hy - hz); h[11] += e + o; h[7] += e - o;
+    }
+
+    // returns den - 1, like collide
+    __device__ static C collide_h(C *h, C ax, C ay, C az, C we, C wo, C &ux, C &uy, C &uz) {
+        constexpr C s0 = 1.0f / 4096.0f;
+        constexpr C w0 = s0 / 3.0f, w1 = s0 / 18.0f, w2 = s0 / 36.0f;
+        const C axis = ((h[2] + h[16]) + (h[6] + h[12])) + (h[8] + h[10]);
+        const C diag = (((h[0] + h[1]) + (h[3] + h[4])) + ((h[14] + h[15]) + (h[17] + h[18]))) +
+                       ((h[5] + h[7]) + (h[11] + h[13]));
+        const C dd = fmaf(w0, h[9], fmaf(w1, axis, w2 * diag));
+        const C jx = fmaf(w1, h[16] - h[2], w2 * (((h[14] + h[15]) + (h[17] + h[18])) - ((h[0] + h[1]) + (h[3] + h[4]))));
+        const C jy = fmaf(w1, h[12] - h[6], w2 * (((h[4] + h[11]) + (h[13] + h[18])) - ((h[0] + h[5]) + (h[7] + h[14]))));
+        const C jz = fmaf(w1, h[10] - h[8], w2 * (((h[3] + h[7]) + (h[13] + h[17])) - ((h[1] + h[5]) + (h[11] + h[15]))));
+        const C den = 1.0f + dd, inv = 1.0f / den;
+        C hx, hy, hz, hxx, hxy, hxz, hyy, hyz, hzz, H0;
+        if (SCH == SCH_REG) {
+            const C dx = ((h[0] + h[1]) + (h[3] + h[4])) + ((h[14] + h[15]) + (h[17] + h[18]));
+            const C dy = ((h[0] + h[4]) + (h[5] + h[7])) + ((h[11] + h[13]) + (h[14] + h[18]));
+            const C dz = ((h[1] + h[3]) + (h[5] + h[7])) + ((h[11] + h[13]) + (h[15] + h[17]));
+            const C pxx = fmaf(w1, h[2] + h[16], w2 * dx);
+            const C pyy = fmaf(w1, h[6] + h[12], w2 * dy);
+            const C pzz = fmaf(w1, h[8] + h[10], w2 * dz);
+            const C pxy = w2 * ((h[0] + h[18]) - (h[4] + h[14]));
+            const C pxz = w2 * ((h[1] + h[17]) - (h[3] + h[15]));
+            const C pyz = w2 * ((h[5] + h[13]) - (h[7] + h[11]));
+            const C d3 = dd * (1.0f / 3.0f);
+            const C c1 = 1.0f - we, c2 = 1.0f - 0.5f * we;
+            const C sx = fmaf(0.5f * ax, den, jx), sy = fmaf(0.5f * ay, den, jy), sz = fmaf(0.5f * az, den, jz);
+            ux = sx * inv; uy = sy * inv; uz = sz * inv;
+            const C rx = den * ux, ry = den * uy, rz = den * uz;
+            H0 = dd;
+            hx = fmaf(c1, jx, fmaf(we, rx, c2 * ax * den));
+            hy = fmaf(c1, jy, fmaf(we, ry, c2 * ay * den));
+            hz = fmaf(c1, jz, fmaf(we, rz, c2 * az * den));
+            hxx = fmaf(c1, pxx - d3, fmaf(we, rx * ux, 2.0f * c2 * ax * sx));
+            hyy = fmaf(c1, pyy - d3, fmaf(we, ry * uy, 2.0f * c2 * ay * sy));
+            hzz = fmaf(c1, pzz - d3, fmaf(we, rz * uz, 2.0f * c2 * az * sz));
+            hxy = fmaf(c1, pxy, fmaf(we, rx * uy, c2 * (ax * sy + ay * sx)));
+            hxz = fmaf(c1, pxz, fmaf(we, rx * uz, c2 * (ax * sz + az * sx)));
+            hyz = fmaf(c1, pyz, fmaf(we, ry * uz, c2 * (ay * sz + az * sy)));
+#pragma unroll
+            for (int q = 0; q < Q; ++q) h[q] = 0.0f;
+            project_h(H0, hx, hy, hz, hxx, hxy, hxz, hyy, hyz, hzz, h);
+            return dd;
+        }
+        ux = fmaf(jx, inv, 0.5f * ax);
+        uy = fmaf(jy, inv, 0.5f * ay);
+        uz = fmaf(jz, inv, 0.5f * az);
+        const C wodd = (SCH == SCH_TRT) ? wo : we;
+        const C c1 = 1.0f - 0.5f * wodd, c2 = 1.0f - 0.5f * we;
+        const C sx = den * ux, sy = den * uy, sz = den * uz;
+        H0 = we * dd;
+        hx = fmaf(wodd, sx, c1 * ax * den);
+        hy = fmaf(wodd, sy, c1 * ay * den);
+        hz = fmaf(wodd, sz, c1 * az * den);
+        const C f2 = 2.0f * c2;
+        hxx = fmaf(we * sx, ux, f2 * ax * sx);
+        hyy = fmaf(we * sy, uy, f2 * ay * sy);
+        hzz = fmaf(we * sz, uz, f2 * az * sz);
+        hxy = fmaf(we * sx, uy, c2 * (ax * sy + ay * sx));
+        hxz = fmaf(we * sx, uz, c2 * (ax * sz + az * sx));
+        hyz = fmaf(we * sy, uz, c2 * (ay * sz + az * sy));
+        if (SCH == SCH_BGK) {
+            const C r = 1.0f - we;
+#pragma unroll
+            for (int q = 0; q < Q; ++q) h[q] *= r;
+        } else {
+            const C c3 = 1.0f - 0.5f * (we + wo), c4 = 0.5f * (we - wo);
+#pragma unroll
+            for (int q = 0; q < 9; ++q) {
+                const C a = h[q], b = h[18 - q];
+                h[q] = c3 * a - c4 * b;
+                h[18 - q] = c3 * b - c4 * a;
+            }
+            h[9] *= (1.0f - we);
+        }
+        project_h(H0, hx, hy, hz, hxx, hxy, hxz, hyy, hyz, hzz, h);
+        return dd;
+    }
+};
+
 } // namespace jlb

@@ -87,6 +87,10 @@ struct StoreF16 {
     }
     template <int q> __device__ static C ldv(S v) { return __half2float(v) * dec<q>(); }
     template <int q> __device__ static void st(S *p, C v) { *p = __float2half_rn(v * enc<q>()); }
+    // the stored value itself, for physics that works on it directly
+    template <int q> __device__ static C ldr(const S *p) { return __half2float(ld_pop(p)); }
+    template <int q> __device__ static C ldvr(S v) { return __half2float(v); }
+    template <int q> __device__ static void str(S *p, C v) { *p = __float2half_rn(v); }
 };
 
 // physics policies whose forcing takes a force density F = F_field + rho g
@@ -98,6 +102,34 @@ template <class PH, class = void> struct uses_force_density {
 template <class PH> struct uses_force_density<PH, std::void_t<decltype(PH::force_density)>> {
     static constexpr bool value = PH::force_density;
 };
+
+// physics policies that collide the stored FP16 values directly (the scale
+// of each weight class folded into the moments and the projection) declare
+// h_space = true and provide collide_h; the bulk of the sites then skips the
+// per-population decode and encode.  Boundary nodes keep the decoded path.
+template <class PH, class = void> struct uses_h_space {
+    static constexpr bool value = false;
+};
+template <class PH> struct uses_h_space<PH, std::void_t<decltype(PH::h_space)>> {
+    static constexpr bool value = PH::h_space;
+};
+template <class ST, class PH, int q> __device__ __forceinline__ typename ST::C bulk_ld(const typename ST::S *p) {
+    if constexpr (uses_h_space<PH>::value) return ST::template ldr<q>(p);
+    else return ST::template ld<q>(p);
+}
+template <class ST, class PH, int q> __device__ __forceinline__ typename ST::C bulk_ldv(typename ST::S v) {
+    if constexpr (uses_h_space<PH>::value) return ST::template ldvr<q>(v);
+    else return ST::template ldv<q>(v);
+}
+template <class ST, class PH, int q> __device__ __forceinline__ void bulk_st(typename ST::S *p, typename ST::C v) {
+    if constexpr (uses_h_space<PH>::value) ST::template str<q>(p, v);
+    else ST::template st<q>(p, v);
+}
+template <class ST, class PH, class C>
+__device__ __forceinline__ C bulk_collide(C *fv, C ax, C ay, C az, C we, C wo, C &ux, C &uy, C &uz) {
+    if constexpr (uses_h_space<PH>::value) return PH::collide_h(fv, ax, ay, az, we, wo, ux, uy, uz);
+    else return PH::collide(fv, ax, ay, az, we, wo, ux, uy, uz);
+}
 
 // compile-time loop
 template <int I, int N> struct Unroll {
@@ -176,7 +208,7 @@ __device__ __forceinline__ void dense_node(const StepArgs &a, int b) {
             const IT e_bb = (IT)q * Np + n;
             e = (m & (1u << q)) ? e_bb : e_reg;
         }
-        fv[q] = ST::template ld<q>(f + e);
+        fv[q] = bulk_ld<ST, PH, q>(f + e);
     });
 
     C ux, uy, uz, rho;
@@ -197,7 +229,7 @@ __device__ __forceinline__ void dense_node(const StepArgs &a, int b) {
         } else {
             ax = (C)a.g[0]; ay = (C)a.g[1]; az = (C)a.g[2];
         }
-        rho = PH::collide(fv, ax, ay, az, (C)a.w_e, (C)a.w_o, ux, uy, uz);
+        rho = bulk_collide<ST, PH>(fv, ax, ay, az, (C)a.w_e, (C)a.w_o, ux, uy, uz);
     }
 
     // scatter: a population heading into a solid is stored back into this
@@ -206,7 +238,7 @@ __device__ __forceinline__ void dense_node(const StepArgs &a, int b) {
     Unroll<0, Q>::run([&]<int q>() {
         IT e;
         if (!PSTEP) {
-            ST::template st<OPP(q)>(fo + ((IT)OPP(q) * Np + n), fv[q]);
+            bulk_st<ST, PH, OPP(q)>(fo + ((IT)OPP(q) * Np + n), fv[q]);
             return;
         }
         if (q == 9) {
@@ -217,7 +249,7 @@ __device__ __forceinline__ void dense_node(const StepArgs &a, int b) {
             const IT e_bb = (IT)OPP(q) * Np + n;
             e = (m & (1u << OPP(q))) ? e_bb : e_reg;
         }
-        ST::template st<q>(fo + e, fv[q]);
+        bulk_st<ST, PH, q>(fo + e, fv[q]);
     });
 
     if (a.write_moments) {
@@ -367,7 +399,7 @@ __device__ __forceinline__ void sparse_node(const StepArgs &a, int b) {
         if (!PSTEP || q == 9) e = (uint32_t)q * Npc + m;
         else if (mk & (1u << q)) e = (uint32_t)q * Npc + m;
         else e = (uint32_t)OPP(q) * Npc + nbr.template operator()<OPP(q)>();
-        fv[q] = ST::template ld<q>(f + e);
+        fv[q] = bulk_ld<ST, PH, q>(f + e);
     });
     C ux, uy, uz;
     C ax, ay, az;
@@ -379,17 +411,17 @@ __device__ __forceinline__ void sparse_node(const StepArgs &a, int b) {
     } else {
         ax = (C)a.g[0]; ay = (C)a.g[1]; az = (C)a.g[2];
     }
-    const C rho = PH::collide(fv, ax, ay, az, (C)a.w_e, (C)a.w_o, ux, uy, uz);
+    const C rho = bulk_collide<ST, PH>(fv, ax, ay, az, (C)a.w_e, (C)a.w_o, ux, uy, uz);
     Unroll<0, Q>::run([&]<int q>() {
         if (!PSTEP) {
-            ST::template st<OPP(q)>(f + ((uint32_t)OPP(q) * Npc + m), fv[q]);
+            bulk_st<ST, PH, OPP(q)>(f + ((uint32_t)OPP(q) * Npc + m), fv[q]);
             return;
         }
         uint32_t e;
         if (q == 9) e = 9u * Npc + m;
         else if (mk & (1u << OPP(q))) e = (uint32_t)OPP(q) * Npc + m;
         else e = (uint32_t)q * Npc + nbr.template operator()<q>();
-        ST::template st<q>(f + e, fv[q]);
+        bulk_st<ST, PH, q>(f + e, fv[q]);
     });
     if (a.write_moments) {
         ((C *)a.den)[n] = rho;

@@ -171,7 +171,7 @@ __global__ void __launch_bounds__(128, JLB_MIN_BLOCKS_TMA) lbm_step_tma_kernel(c
             // inside the slot's segment even where it is not the right value)
             Unroll<0, Q>::run([&]<int q>() {
                 constexpr int sh = (PSTEP && q != 9) ? CZ(q) : 0;
-                fv[q] = ST::template ldv<q>(cur[q * G::SEG + G::PAD + t - sh]);
+                fv[q] = bulk_ldv<ST, PH, q>(cur[q * G::SEG + G::PAD + t - sh]);
             });
             // rare lanes fix theirs up from global memory: links that bounce
             // back read their own opposite slot; sources that wrap in k
@@ -181,10 +181,10 @@ __global__ void __launch_bounds__(128, JLB_MIN_BLOCKS_TMA) lbm_step_tma_kernel(c
                     if (q == 9) return;
                     const int kk = k - CZ(q);
                     if (m & (1u << q)) {
-                        fv[q] = ST::template ld<q>(f + ((int32_t)q * Np + n));
+                        fv[q] = bulk_ld<ST, PH, q>(f + ((int32_t)q * Np + n));
                     } else if (kk < 0 || kk >= a.nz) {
                         const int32_t src = n + dI[1 - CX(q)] + dJ[1 - CY(q)] + dK[1 - CZ(q)];
-                        fv[q] = ST::template ld<q>(f + ((int32_t)OPP(q) * Np + src));
+                        fv[q] = bulk_ld<ST, PH, q>(f + ((int32_t)OPP(q) * Np + src));
                     }
                 });
             }
@@ -198,10 +198,10 @@ __global__ void __launch_bounds__(128, JLB_MIN_BLOCKS_TMA) lbm_step_tma_kernel(c
                 ax = (C)a.g[0]; ay = (C)a.g[1]; az = (C)a.g[2];
             }
             C ux, uy, uz;
-            const C rho = PH::collide(fv, ax, ay, az, (C)a.w_e, (C)a.w_o, ux, uy, uz);
+            const C rho = bulk_collide<ST, PH>(fv, ax, ay, az, (C)a.w_e, (C)a.w_o, ux, uy, uz);
             Unroll<0, Q>::run([&]<int q>() {
                 if (!PSTEP) {
-                    ST::template st<OPP(q)>(f + ((int32_t)OPP(q) * Np + n), fv[q]);
+                    bulk_st<ST, PH, OPP(q)>(f + ((int32_t)OPP(q) * Np + n), fv[q]);
                     return;
                 }
                 int32_t e;
@@ -211,7 +211,7 @@ __global__ void __launch_bounds__(128, JLB_MIN_BLOCKS_TMA) lbm_step_tma_kernel(c
                     const int32_t dst = n + dI[1 + CX(q)] + dJ[1 + CY(q)] + dK[1 + CZ(q)];
                     e = (m & (1u << OPP(q))) ? ((int32_t)OPP(q) * Np + n) : ((int32_t)q * Np + dst);
                 }
-                ST::template st<q>(f + e, fv[q]);
+                bulk_st<ST, PH, q>(f + e, fv[q]);
             });
             if (a.write_moments) {
                 ((C *)a.den)[n] = rho;
