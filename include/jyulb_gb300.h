@@ -153,6 +153,13 @@ int jlb_set_populations(jlb_solver *s, const double *f);
  * out[7] = number of non-finite den/u values found. */
 int jlb_reduce(jlb_solver *s, double out[8]);
 
+/* Steady-state convergence residual of the last moment-writing step:
+ * *res = ||u - u_prev|| / ||u|| over fluid sites (L2 norms, FP64 sums on the
+ * GPU), where u_prev is the velocity at the previous call (zero before the
+ * first one, which therefore returns 1 unless u = 0).  No reference
+ * counterpart; the examples track convergence through printed sums. */
+int jlb_residual(jlb_solver *s, double *res);
+
 /* Flow information of the last moment-writing step, as the C++ executable's
  * IsothermalSolver::calc_flow_info (include/solver/solver.cpp:64-129)
  * computes it over fluid sites, in the column order of its .evol file

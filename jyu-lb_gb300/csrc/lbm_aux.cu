@@ -300,6 +300,44 @@ __global__ void reduce_final_kernel(const double *partial, int nblocks, double *
     if (lane == 0) out[c] = v;
 }
 
+// steady-state convergence residual: over fluid sites, FP64 sums of
+// |u - u_prev|^2 (slot 0) and |u|^2 (slot 1) against the velocity kept at
+// the previous call, which the same pass replaces by the current one;
+// reduce_final_kernel combines the per-block partials (8 slots per block)
+template <class C>
+__global__ void __launch_bounds__(RED_THREADS) residual_partial_kernel(AuxGeom g, const uint32_t *nmask,
+                                                                       const C *ux, const C *uy, const C *uz,
+                                                                       C *prev, double *partial) {
+    double d2 = 0.0, u2 = 0.0;
+    for (int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; n < g.N;
+         n += (int64_t)gridDim.x * blockDim.x) {
+        if (nmask[n] & MASK_SOLID) continue;
+        const C v[3] = {ux[n], uy[n], uz[n]};
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const double u = (double)v[c], d = u - (double)prev[c * g.Np + n];
+            d2 += d * d;
+            u2 += u * u;
+            prev[c * g.Np + n] = v[c];
+        }
+    }
+    __shared__ double sm[2][RED_THREADS / 32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        d2 += __shfl_down_sync(0xffffffffu, d2, o);
+        u2 += __shfl_down_sync(0xffffffffu, u2, o);
+    }
+    if (lane == 0) { sm[0][wid] = d2; sm[1][wid] = u2; }
+    __syncthreads();
+    if (threadIdx.x < 8) {
+        double v = 0.0;
+        if (threadIdx.x < 2)
+            for (int w = 0; w < RED_THREADS / 32; ++w) v += sm[threadIdx.x][w];
+        partial[(int64_t)blockIdx.x * 8 + threadIdx.x] = v;
+    }
+}
+
 // ---------------------------------------------------------------------------
 // flow information (the C++ executable's IsothermalSolver::calc_flow_info,
 // include/solver/solver.cpp:64-129): over fluid sites, sums of den, j = den u,
@@ -569,6 +607,18 @@ int aux_reduce(int prec, const AuxGeom &g, const uint32_t *nmask, const void *de
     else
         reduce_partial_kernel<float, true><<<nblocks, RED_THREADS, 0, st>>>(
             g, nmask, (const float *)den, (const float *)ux, (const float *)uy, (const float *)uz, partial);
+    reduce_final_kernel<<<1, 256, 0, st>>>(partial, nblocks, out);
+    return (int)cudaGetLastError();
+}
+
+int aux_residual(int prec, const AuxGeom &g, const uint32_t *nmask, const void *ux, const void *uy,
+                 const void *uz, void *prev, double *partial, int nblocks, double *out, cudaStream_t st) {
+    if (prec == PREC_FP64)
+        residual_partial_kernel<double><<<nblocks, RED_THREADS, 0, st>>>(
+            g, nmask, (const double *)ux, (const double *)uy, (const double *)uz, (double *)prev, partial);
+    else
+        residual_partial_kernel<float><<<nblocks, RED_THREADS, 0, st>>>(
+            g, nmask, (const float *)ux, (const float *)uy, (const float *)uz, (float *)prev, partial);
     reduce_final_kernel<<<1, 256, 0, st>>>(partial, nblocks, out);
     return (int)cudaGetLastError();
 }

@@ -56,6 +56,11 @@ int aux_reduce_blocks(int64_t N);
 // partial must hold 8 * nblocks doubles; out 8 doubles (device)
 int aux_reduce(int prec, const AuxGeom &g, const uint32_t *nmask, const void *den, const void *ux,
                const void *uy, const void *uz, double *partial, int nblocks, double *out, cudaStream_t st);
+// convergence residual: out[0] = sum |u - prev|^2, out[1] = sum |u|^2 over
+// fluid sites (FP64); prev (3 * Np, compute type) then holds u.  partial as
+// for aux_reduce
+int aux_residual(int prec, const AuxGeom &g, const uint32_t *nmask, const void *ux, const void *uy,
+                 const void *uz, void *prev, double *partial, int nblocks, double *out, cudaStream_t st);
 // flow information: partial must hold 12 * nblocks doubles; out 12 doubles
 // (device): sums den, jx, jy, jz, |j|, ux, uy, uz, |u|; max den, min den, max |u|
 int aux_flow_info(int prec, const AuxGeom &g, const uint32_t *nmask, const void *den, const void *ux,

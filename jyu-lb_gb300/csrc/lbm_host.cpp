@@ -72,6 +72,7 @@ struct jlb_solver {
     double *red_partial = nullptr, *red_out = nullptr;
     int red_blocks = 0;
     double *fi_partial = nullptr, *fi_out = nullptr; // flow information (allocated on first use)
+    void *res_prev = nullptr;        // velocity at the last residual call (3 * Np, compute type)
     double *stg_den = nullptr, *stg_vel = nullptr;   // device copies of the host den/vel layout (DMA download)
     bool stg_failed = false;
     cudaStream_t st2 = nullptr;          // download stream of the overlapped last step
@@ -1206,7 +1207,7 @@ void jlb_destroy(jlb_solver *s) {
                     s->red_out, s->d_sp_node, s->d_sp_info, s->d_sp_rd, s->d_sp_wr, s->d_sp_lw, s->d_sp_bc,
                     s->d_sp_den, s->d_err, s->fi_partial, s->fi_out, s->stg_den, s->stg_vel,
                     s->fc, s->d_csite, s->d_cidx, s->d_sp_rd_c, s->d_sp_wr_c, s->d_sp_cnode,
-                    s->d_wall_pos, s->d_wall_vel};
+                    s->d_wall_pos, s->d_wall_vel, s->res_prev};
     for (void *p : bufs)
         if (p) cudaFree(p);
     if (s->pinned) cudaFreeHost(s->pinned);
@@ -1452,6 +1453,25 @@ int jlb_reduce(jlb_solver *s, double out[8]) {
     CK(cudaMemcpyAsync(out, s->red_out, 8 * sizeof(double), cudaMemcpyDeviceToHost, s->st));
     CK(cudaStreamSynchronize(s->st));
     if (out[7] != 0.0) return fail(s, JLB_ERR_NUMERIC, "non-finite density or velocity found");
+    return JLB_OK;
+}
+
+int jlb_residual(jlb_solver *s, double *res) {
+    if (!s || !res) return fail(s, JLB_ERR_INVALID_ARG, "NULL argument");
+    if (!s->init_done) return fail(s, JLB_ERR_STATE, "finalize_init has not been called");
+    if (!s->res_prev) {
+        const size_t nb = (size_t)3 * s->Np * s->csz;
+        CK(cudaMalloc(&s->res_prev, nb));
+        CK(cudaMemsetAsync(s->res_prev, 0, nb, s->st));
+    }
+    CKR(aux_residual(s->prec, s->geom, s->nmask, s->mom[1], s->mom[2], s->mom[3], s->res_prev, s->red_partial,
+                     s->red_blocks, s->red_out, s->st));
+    s->launches += 2;
+    double v[2];
+    CK(cudaMemcpyAsync(v, s->red_out, sizeof(v), cudaMemcpyDeviceToHost, s->st));
+    CK(cudaStreamSynchronize(s->st));
+    if (!std::isfinite(v[0]) || !std::isfinite(v[1])) return fail(s, JLB_ERR_NUMERIC, "non-finite velocity found");
+    *res = v[1] > 0.0 ? std::sqrt(v[0] / v[1]) : (v[0] > 0.0 ? 1.0 : 0.0);
     return JLB_OK;
 }
 

@@ -24,7 +24,7 @@ JLB_ERR_NUMERIC = -6
 EXPORTED_SYMBOLS = (
     "jlb_check_config", "jlb_create", "jlb_destroy", "jlb_finalize_init", "jlb_set_acc", "jlb_set_static_halo", "jlb_evolve",
     "jlb_step", "jlb_download_moments", "jlb_get_populations", "jlb_set_populations",
-    "jlb_reduce", "jlb_flow_info", "jlb_reduce_moments_noalloc", "jlb_tot_tsteps", "jlb_rlx_prm", "jlb_kernel_launches",
+    "jlb_reduce", "jlb_residual", "jlb_flow_info", "jlb_reduce_moments_noalloc", "jlb_tot_tsteps", "jlb_rlx_prm", "jlb_kernel_launches",
     "jlb_transfer_bytes", "jlb_host_timers",
     "jlb_last_error", "jlb_batch_create", "jlb_batch_destroy", "jlb_batch_step", "jlb_batch_moments",
     "jlb_batch_populations", "jlb_batch_info", "jlb_batch_domain_fluid", "jlb_batch_last_error",
@@ -99,6 +99,7 @@ def load() -> ctypes.CDLL:
         "jlb_get_populations": (ctypes.c_int, [vp, dp]),
         "jlb_set_populations": (ctypes.c_int, [vp, dp]),
         "jlb_reduce": (ctypes.c_int, [vp, dp]),
+        "jlb_residual": (ctypes.c_int, [vp, dp]),
         "jlb_flow_info": (ctypes.c_int, [vp, ctypes.c_double, dp]),
         "jlb_reduce_moments_noalloc": (ctypes.c_int, [vp, vp, vp, vp, vp, ctypes.c_int64, ctypes.c_int32,
                                                       vp, vp]),

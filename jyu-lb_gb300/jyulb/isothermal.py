@@ -366,6 +366,17 @@ class Solver:
             self._raise(rc)
         return {'mass': out[0], 'momentum': out[1:4].copy(), 'vel_sum': out[4:7].copy()}
 
+    def residual(self):
+        """Steady-state convergence residual ||u - u_prev|| / ||u|| over fluid
+        sites, u_prev being the velocity at the previous call (zero before
+        the first); FP64 sums on the GPU."""
+        self._need_init()
+        out = np.zeros(1)
+        rc = self._lib.jlb_residual(self._h, _native.dptr(out))
+        if rc != _native.JLB_OK:
+            self._raise(rc)
+        return float(out[0])
+
     FLOW_INFO_KEYS = ('tot_den', 'tot_jx', 'tot_jy', 'tot_jz', 'tot_j2', 'ave_ux', 'ave_uy', 'ave_uz', 'ave_u2',
                       'max_u2', 'max_den', 'min_den')
 

@@ -52,3 +52,36 @@ def test_fp32_profile_close_to_reference(name):
     ref = np.array([[float.fromhex(v) for v in row] for row in GOLD[name]["profile"]])
     assert np.abs(prof - ref).max() <= 1e-4 * np.abs(ref).max()
     assert abs(err - float.fromhex(GOLD[name]["error"])) <= 5e-5, err
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_convergence_residual(precision):
+    # Solver.residual() = ||u - u_prev|| / ||u|| over fluid sites (FP64 sums
+    # on the GPU) equals the same quantity from the downloaded fields, and
+    # falls as the gravity channel (H = 11, nu = 0.2/6: diffusion time
+    # H^2/nu ~ 3600 steps) reaches its steady state over 20 calls of 500 steps
+    from jyulb import flow_field
+    from jyulb.isothermal import Solver
+
+    c = next(c for c in pc.cases() if c["name"] == "poiseuille_grav")
+    s = Solver(np.array(c["lat"], dtype=np.int32), c["scheme"], c["kvisc"], pc.gravity(c),
+               np.array(c["bc"], dtype=np.int32), precision=precision)
+    pc.setup(s, c, flow_field)
+    s.finalize_init()
+    fl = np.asarray(s.get_phase()) != 0
+    s.evolve(10)
+    u_prev = np.array(s.get_vel())[fl]
+    assert s.residual() == 1.0
+    res = []
+    for _ in range(20):
+        s.evolve(500)
+        u = np.array(s.get_vel())[fl]
+        host = np.sqrt(((u - u_prev) ** 2).sum() / (u ** 2).sum())
+        r = s.residual()
+        assert r == pytest.approx(host, rel=1e-12, abs=1e-300)
+        res.append(r)
+        u_prev = u
+    # the transient decays by about e^-1.4 per call until FP32 rounding sets
+    # the floor
+    assert all(b < a for a, b in zip(res[:5], res[1:6])), res
+    assert res[-1] < (1e-6 if precision == 0 else 1e-4), res
