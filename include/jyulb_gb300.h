@@ -234,7 +234,7 @@ const char *jlb_batch_last_error(const jlb_batch *b);
 /* ---------------------------------------------------------------------
  * Discrete adjoint of the time step (no counterpart in the reference, which
  * has no derivatives).  A problem is a domain described by a jlb_config:
- * BGK or TRT, FP64 or FP32, started from rest; its parameters are the relaxation time
+ * BGK, TRT or regularized, FP64 or FP32, started from rest; its parameters are the relaxation time
  * tau, the body force g and the u_x of each site of a FIXED_VEL face 1X.
  * The loss is sum |u - target|^2 of the stored velocity on the plane
  * x = loss_plane after the last step.  The forward run keeps checkpoints

@@ -19,9 +19,12 @@
 //   f*_q = c3 g_q - c4 g_opp(q) + P_q(H),  f*_rest = (1 - we) g_rest + P_rest(H),
 // with c1 = 1 - wo/2, c2 = 1 - we/2, c3 = 1 - (we + wo)/2, c4 = (we - wo)/2
 // (BGK: wo = we) and P_q(H) = w_q (H0 + 3 c.H1 + 4.5 (c c - I/3):H2).
-// Its transpose and the local sensitivities to we, wo and a are written out
-// below.  Zou-He is affine in the populations and in j, so its transpose is
-// read off the forward assignment applied to unit vectors.
+// Regularized (jyulb/D3Q19.pyx:859-940): f* = P(H) with
+//   H0 = rho, H1 = j + rho a, H2 = (1 - we) (Pi - rho I/3) + we s s / rho + c2 (a s + s a),
+// Pi = sum c c g the second moment of the inputs.
+// Their transposes and the local sensitivities to we, wo and a are written
+// out below.  Zou-He is affine in the populations and in j, so its transpose
+// is read off the forward assignment applied to unit vectors.
 #include "lbm_adjoint.h"
 #include "lbm_step.cuh"
 
@@ -171,8 +174,9 @@ __device__ void zh_adjoint(int fc, int kind, double den, double ux, double uy, d
 // forms the adjoint of every input li_q (handed to `put`) and adds the local
 // sensitivities to we, wo, ax, ay, az into pg.  On the loss step a site of the
 // loss plane adds the seed dL/du of its stored velocity u = j/rho + a/2.
-template <class C, bool SHIFTED> struct AdjSums {
+template <class C, bool SHIFTED, bool PI = false> struct AdjSums {
     C rho = SHIFTED ? (C)1 : (C)0, jx = 0, jy = 0, jz = 0;
+    C pxx = 0, pyy = 0, pzz = 0, pxy = 0, pxz = 0, pyz = 0; // sum c c g (PI: regularized)
     C L0 = 0, L1x = 0, L1y = 0, L1z = 0, Lxx = 0, Lyy = 0, Lzz = 0, Lxy = 0, Lxz = 0, Lyz = 0;
     C sum_pair = 0; // sum_q lo_q (f_q + f_opp(q)), q != rest
     C dif_pair = 0; // sum_q lo_q (f_opp(q) - f_q)
@@ -185,6 +189,14 @@ template <class C, bool SHIFTED> struct AdjSums {
         if (cx) jx += (C)cx * g;
         if (cy) jy += (C)cy * g;
         if (cz) jz += (C)cz * g;
+        if constexpr (PI) {
+            if (cx) pxx += g;
+            if (cy) pyy += g;
+            if (cz) pzz += g;
+            if (cx * cy) pxy += (C)(cx * cy) * g;
+            if (cx * cz) pxz += (C)(cx * cz) * g;
+            if (cy * cz) pyz += (C)(cy * cz) * g;
+        }
         const C wl = w * l;
         L0 += wl;
         if (cx) L1x += (C)(3 * cx) * wl;
@@ -207,16 +219,16 @@ template <class C, bool SHIFTED> struct AdjSums {
 };
 
 // adds the population pair sums once all 19 inputs and adjoints are at hand
-template <class C, bool SHIFTED>
-__device__ __forceinline__ void adj_accumulate(AdjSums<C, SHIFTED> &S, const C *g, const C *lo) {
+template <class C, bool SHIFTED, bool PI>
+__device__ __forceinline__ void adj_accumulate(AdjSums<C, SHIFTED, PI> &S, const C *g, const C *lo) {
     Unroll<0, Q>::run([&]<int q>() { S.template add<q>(g[q], lo[q]); });
     Unroll<0, 9>::run([&]<int q>() { S.template pair<q>(g[q], g[OPP(q)], lo[q], lo[OPP(q)]); });
 }
 
-template <class C, bool SHIFTED, int SCH, bool SEED, class PUT>
-__device__ __forceinline__ void adj_finish(const AdjSums<C, SHIFTED> &S, const C *lo, C ax, C ay, C az, C we, C wo,
-                                           C *pg, bool on_plane, const double *tg, double gx, double gy, double gz,
-                                           PUT &&put) {
+template <class C, bool SHIFTED, int SCH, bool SEED, bool PI, class PUT>
+__device__ __forceinline__ void adj_finish(const AdjSums<C, SHIFTED, PI> &S, const C *lo, C ax, C ay, C az, C we,
+                                           C wo, C *pg, bool on_plane, const double *tg, double gx, double gy,
+                                           double gz, PUT &&put) {
     if (SCH == SCH_BGK) wo = we;
     const C rho = S.rho, jx = S.jx, jy = S.jy, jz = S.jz;
     const C c1 = (C)1 - (C)0.5 * wo, c2 = (C)1 - (C)0.5 * we;
@@ -234,8 +246,8 @@ __device__ __forceinline__ void adj_finish(const AdjSums<C, SHIFTED> &S, const C
     const C dsz = wo * S.L1z + (C)2 * we * Lsz * ir + (C)2 * c2 * Laz;
     const C sLs = sx * Lsx + sy * Lsy + sz * Lsz;
     const C L1a = S.L1x * ax + S.L1y * ay + S.L1z * az;
-    C drho = we * S.L0 + c1 * L1a - we * sLs * ir * ir + (C)0.5 * (ax * dsx + ay * dsy + az * dsz);
-    C djx = dsx, djy = dsy, djz = dsz;
+    // the loss's own dependence on this site's rho and j (seeding step)
+    C sd_rho = 0, sd_jx = 0, sd_jy = 0, sd_jz = 0;
     C dax_seed = 0, day_seed = 0, daz_seed = 0;
     if (SEED && on_plane) {
         // L = sum |u - target|^2 over the plane
@@ -243,9 +255,50 @@ __device__ __forceinline__ void adj_finish(const AdjSums<C, SHIFTED> &S, const C
         const C d0 = (C)(2.0 * ((double)ux + 0.5 * gx - tg[0]));
         const C d1 = (C)(2.0 * ((double)uy + 0.5 * gy - tg[1]));
         const C d2 = (C)(2.0 * ((double)uz + 0.5 * gz - tg[2]));
-        djx += d0 * ir; djy += d1 * ir; djz += d2 * ir;
-        drho -= (d0 * ux + d1 * uy + d2 * uz) * ir;
+        sd_jx = d0 * ir; sd_jy = d1 * ir; sd_jz = d2 * ir;
+        sd_rho = -(d0 * ux + d1 * uy + d2 * uz) * ir;
         dax_seed = (C)0.5 * d0; day_seed = (C)0.5 * d1; daz_seed = (C)0.5 * d2;
+    }
+    const C drho = we * S.L0 + c1 * L1a - we * sLs * ir * ir + (C)0.5 * (ax * dsx + ay * dsy + az * dsz) + sd_rho;
+    const C djx = dsx + sd_jx, djy = dsy + sd_jy, djz = dsz + sd_jz;
+    if constexpr (SCH == SCH_REG) {
+        // lam_q = K + d . c_q + (1 - we) c_q.M.c_q with M the output-adjoint
+        // second moments (Lxx .. Lyz); no relaxation term (the projection
+        // drops the non-hydrodynamic part)
+        const C c1r = (C)1 - we;
+        const C trM = S.Lxx + S.Lyy + S.Lzz;
+        const C aLs = ax * Lsx + ay * Lsy + az * Lsz;
+        const C aLa = ax * Lax + ay * Lay + az * Laz;
+        const C K = S.L0 + L1a - c1r * trM * (C)(1.0 / 3.0) + we * (aLs * ir - sLs * ir * ir) + c2 * aLa + sd_rho;
+        const C dx = S.L1x + (C)2 * we * Lsx * ir + (C)2 * c2 * Lax + sd_jx;
+        const C dy = S.L1y + (C)2 * we * Lsy * ir + (C)2 * c2 * Lay + sd_jy;
+        const C dz = S.L1z + (C)2 * we * Lsz * ir + (C)2 * c2 * Laz + sd_jz;
+        Unroll<0, Q>::run([&]<int q>() {
+            constexpr int cx = CX(q), cy = CY(q), cz = CZ(q);
+            C v = K;
+            if (cx) v += (C)cx * dx;
+            if (cy) v += (C)cy * dy;
+            if (cz) v += (C)cz * dz;
+            C cmc = 0;
+            if (cx) cmc += S.Lxx;
+            if (cy) cmc += S.Lyy;
+            if (cz) cmc += S.Lzz;
+            if (cx * cy) cmc += (C)(2 * cx * cy) * S.Lxy;
+            if (cx * cz) cmc += (C)(2 * cx * cz) * S.Lxz;
+            if (cy * cz) cmc += (C)(2 * cy * cz) * S.Lyz;
+            v += c1r * cmc;
+            put.template operator()<q>(v);
+        });
+        // M:(Pi - rho I/3), the input's second moment (shifted populations
+        // carry rho - 1 in rho - 1 and the same deviatoric moments)
+        const C r3 = (SHIFTED ? (S.rho - (C)1) : S.rho) * (C)(1.0 / 3.0);
+        const C MP = S.Lxx * (S.pxx - r3) + S.Lyy * (S.pyy - r3) + S.Lzz * (S.pzz - r3) +
+                     (C)2 * (S.Lxy * S.pxy + S.Lxz * S.pxz + S.Lyz * S.pyz);
+        pg[0] += -MP + sLs * ir - aLs;
+        pg[2] += rho * S.L1x + (we + (C)2 * c2) * Lsx + c2 * rho * Lax + dax_seed;
+        pg[3] += rho * S.L1y + (we + (C)2 * c2) * Lsy + c2 * rho * Lay + day_seed;
+        pg[4] += rho * S.L1z + (we + (C)2 * c2) * Lsz + c2 * rho * Laz + daz_seed;
+        return;
     }
     Unroll<0, Q>::run([&]<int q>() {
         constexpr int cx = CX(q), cy = CY(q), cz = CZ(q);
@@ -284,9 +337,6 @@ template <class C> __device__ __forceinline__ void block_sensitivities(C *pg, do
     if (tid < 5) slot[tid] += (double)sm[tid][0] + (double)sm[tid][1] + (double)sm[tid][2] + (double)sm[tid][3];
 }
 
-// resident blocks per SM the dense kernel is compiled for: the FP32 sweep
-// fits 5 x 128 threads (<= 96 registers) without spills; the loss-seeding
-// variant, which runs once per sweep, gets 4
 // resident 128-thread blocks per SM asked of the register allocator (the
 // seeding launch, which also forms the loss gradient, gets one fewer)
 #ifndef JLB_ADJ_MIN_BLOCKS
@@ -344,7 +394,7 @@ __device__ __forceinline__ void adjoint_dense_sites(const AdjArgs &A, int b, typ
                 const IT dst = n + dI[1 + CX(q)] + dJ[1 + CY(q)] + dK[1 + CZ(q)];
                 return (m & (1u << OPP(q))) ? (IT)OPP(q) * Np + n : (IT)q * Np + dst;
             };
-            AdjSums<C, ST::shifted> sums;
+            AdjSums<C, ST::shifted, SCH == SCH_REG> sums;
             C lo[Q];
             {
                 C g[Q];
@@ -390,7 +440,7 @@ __device__ __forceinline__ void adjoint_boundary_sites(const AdjArgs &A, int b, 
         const double *tg = nullptr;
         const bool on_plane = SEED && i == A.plane;
         if (on_plane) tg = A.target + 3 * ((int64_t)j * a.nz + k);
-        AdjSums<C, ST::shifted> sums;
+        AdjSums<C, ST::shifted, SCH == SCH_REG> sums;
         adj_accumulate(sums, g, lo);
         adj_finish<C, ST::shifted, SCH, SEED>(sums, lo, (C)a.g[0], (C)a.g[1], (C)a.g[2], (C)a.w_e, (C)a.w_o, pg, on_plane,
                                              tg, a.g[0], a.g[1], a.g[2], [&]<int q>(C v) { li[q] = v; });
@@ -450,10 +500,12 @@ int launch_adjoint_scheme(const AdjArgs &A, bool pstep, bool seed, cudaStream_t 
 int launch_adjoint_step(const AdjArgs &A, int prec, int scheme, bool pstep, cudaStream_t st) {
     const bool seed = A.seed != 0;
     if (prec == PREC_FP64)
-        return scheme == SCH_TRT ? launch_adjoint_scheme<StoreF64, SCH_TRT>(A, pstep, seed, st)
-                                 : launch_adjoint_scheme<StoreF64, SCH_BGK>(A, pstep, seed, st);
-    return scheme == SCH_TRT ? launch_adjoint_scheme<StoreF32, SCH_TRT>(A, pstep, seed, st)
-                             : launch_adjoint_scheme<StoreF32, SCH_BGK>(A, pstep, seed, st);
+        return scheme == SCH_TRT   ? launch_adjoint_scheme<StoreF64, SCH_TRT>(A, pstep, seed, st)
+               : scheme == SCH_REG ? launch_adjoint_scheme<StoreF64, SCH_REG>(A, pstep, seed, st)
+                                   : launch_adjoint_scheme<StoreF64, SCH_BGK>(A, pstep, seed, st);
+    return scheme == SCH_TRT   ? launch_adjoint_scheme<StoreF32, SCH_TRT>(A, pstep, seed, st)
+           : scheme == SCH_REG ? launch_adjoint_scheme<StoreF32, SCH_REG>(A, pstep, seed, st)
+                               : launch_adjoint_scheme<StoreF32, SCH_BGK>(A, pstep, seed, st);
 }
 
 } // namespace jlb

@@ -1,6 +1,6 @@
 """Gradients of a velocity-field loss through the D3Q19 time step.
 
-``ChannelProblem`` is a domain (BGK or TRT, FP32-shifted or FP64) started from
+``ChannelProblem`` is a domain (BGK, TRT or regularized; FP32-shifted or FP64) started from
 rest, with a FIXED_VEL inlet on face 1X whose u_x is a parameter per inlet
 site.  The forward run advances ``steps`` steps and scores the stored velocity
 on the plane x = ``loss_plane``:  L = sum over fluid sites of |u - target|^2.

@@ -41,16 +41,18 @@ def torch_grads(phase, tau, g, uin, target, steps, plane, scheme, magic, zwall=F
     return float(L.detach()), float(t_tau.grad), t_g.grad.numpy(), t_uin.grad.numpy()
 
 
-@pytest.mark.parametrize("scheme,zwall", [("TRT", False), ("BGK", False), ("TRT", True)])
+@pytest.mark.parametrize("scheme,zwall", [("TRT", False), ("BGK", False), ("TRT", True), ("REG", False),
+                                          ("REG", True)])
 def test_fp64_adjoint_matches_torch_autograd(scheme, zwall):
     from jyulb.adjoint import ChannelProblem
-    from jyulb.defs import BGK, FIXED_DEN, FIXED_VEL, FP64, PERIODIC, TRT, WALL
+    from jyulb.defs import BGK, FIXED_DEN, FIXED_VEL, FP64, PERIODIC, REGULARIZATION, TRT, WALL
 
     phase, uin, target = setup(1)
     tau, g, steps, plane = 0.8, np.array([1e-5, 2e-6, 1e-6 if zwall else 0.0]), 30, 12
     magic = 0.25 if scheme == "TRT" else None
     zb = WALL if zwall else PERIODIC
-    p = ChannelProblem(phase, bc=[FIXED_VEL, FIXED_DEN, WALL, WALL, zb, zb], rlx_scheme=TRT if scheme == "TRT" else BGK,
+    sch = {"TRT": TRT, "BGK": BGK, "REG": REGULARIZATION}[scheme]
+    p = ChannelProblem(phase, bc=[FIXED_VEL, FIXED_DEN, WALL, WALL, zb, zb], rlx_scheme=sch,
                        precision=FP64, trt_magic=magic, loss_plane=plane, checkpoint_every=7)
     L, _ = p.forward(tau, g, uin, steps, target)
     dtau, dg, duin = p.backward()
@@ -61,18 +63,20 @@ def test_fp64_adjoint_matches_torch_autograd(scheme, zwall):
     np.testing.assert_allclose(duin, duin_t, rtol=1e-7, atol=1e-9 * np.abs(duin_t).max())
 
 
+@pytest.mark.parametrize("scheme", [1, 2])
 @pytest.mark.parametrize("precision,tol", [(0, 1e-6), (1, 2e-3)])
-def test_adjoint_matches_central_differences(precision, tol):
+def test_adjoint_matches_central_differences(precision, tol, scheme):
     from jyulb.adjoint import ChannelProblem
-    from jyulb.defs import FP64, TRT
+    from jyulb.defs import FP64
 
     phase, uin, target = setup(2, shape=(20, 12, 4))
     tau, g, steps, plane = 0.7, np.array([5e-6, 0.0, 0.0]), 40, 15
-    p = ChannelProblem(phase, rlx_scheme=TRT, precision=precision, trt_magic=0.25, loss_plane=plane,
+    magic = 0.25 if scheme == 1 else None
+    p = ChannelProblem(phase, rlx_scheme=scheme, precision=precision, trt_magic=magic, loss_plane=plane,
                        checkpoint_every=8)
     p.forward(tau, g, uin, steps, target)
     dtau, dg, duin = p.backward()
-    ref = ChannelProblem(phase, rlx_scheme=TRT, precision=FP64, trt_magic=0.25, loss_plane=plane,
+    ref = ChannelProblem(phase, rlx_scheme=scheme, precision=FP64, trt_magic=magic, loss_plane=plane,
                          checkpoint_every=8)
 
     def L(tau_, g_, uin_):

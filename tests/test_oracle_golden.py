@@ -55,3 +55,33 @@ def test_oracle_steady_profiles_match_reference():
         ref = np.array([[float.fromhex(v) for v in row] for row in gold[c["name"]]["profile"]])
         np.testing.assert_array_equal(prof, ref, err_msg=c["name"])
         assert pc.error(prof, c, flow_field) == float.fromhex(gold[c["name"]]["error"])
+
+
+@pytest.mark.parametrize("scheme", ["BGK", "TRT", "REG"])
+def test_torch_step_matches_oracle(scheme):
+    # the pure-torch FP64 step that checks the adjoint's gradients reproduces
+    # the oracle (and so the reference) on its channel: Zou-He velocity inlet
+    # with a per-site u_x, density outlet, walls in y, periodic z, a cylinder
+    import torch
+
+    from pyoracle import Oracle
+    from torch_lbm import run
+
+    rng = np.random.default_rng(4)
+    nx, ny, nz = 12, 8, 4
+    X, Y = np.meshgrid(np.arange(nx), np.arange(ny), indexing="ij")
+    phase = np.ones((nx, ny, nz), np.uint8)
+    phase[(X - 5) ** 2 + (Y - 4) ** 2 <= 2.0] = 0
+    uin = 0.02 + 0.005 * rng.standard_normal((ny, nz))
+    tau, g, steps = 0.8, np.array([1e-5, 2e-6, 0.0]), 25
+    sch = {"BGK": 0, "TRT": 1, "REG": 2}[scheme]
+    u = run(phase, torch.tensor(tau, dtype=torch.float64), torch.tensor(g), torch.tensor(uin), steps,
+            scheme=scheme).numpy()
+    o = Oracle([nx, ny, nz], sch, (tau - 0.5) / 3.0, list(g), [3, 2, 0, 0, 1, 1])
+    o.get_phase()[:] = phase
+    o.finalize_init()  # from rest, as the torch step starts
+    o.get_vel()[0, :, :, 0] = uin  # inlet data, read at the evolve call
+    o.evolve(steps)
+    fl = phase != 0
+    ref = np.moveaxis(o.get_vel(), -1, 0)[:, fl]
+    np.testing.assert_allclose(u[:, fl], ref, rtol=0, atol=1e-13 * np.abs(ref).max())

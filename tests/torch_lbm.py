@@ -2,8 +2,8 @@
 
 TEST INFRASTRUCTURE ONLY.  Pull streaming with halfway bounce-back and
 periodic wrap, Zou-He velocity inlet on face 1X (per-site u_x) and density
-outlet on face X1, TRT (or BGK) collision with forcing -- the physics of
-jyulb/isothermal.pyx:1112-1326 and jyulb/D3Q19.pyx:655-853 -- written with
+outlet on face X1, TRT, BGK or regularized collision with forcing -- the
+physics of jyulb/isothermal.pyx:1112-1326 and jyulb/D3Q19.pyx:655-940 -- written with
 differentiable tensor operations so that torch autograd yields reference
 gradients of the plane-velocity loss.
 """
@@ -110,6 +110,29 @@ def collide(g, a, we, wo):
     return relax + P, rho, u
 
 
+def collide_reg(g, a, we):
+    """Regularized collision (jyulb/D3Q19.pyx:859-940): f* = P(H) with H0 = rho,
+    H1 = j + rho a, H2 = (1 - we)(Pi - rho I/3) + we s s / rho + c2 (a s + s a)."""
+    C = torch.tensor([CI, CJ, CK], dtype=g.dtype, device=g.device)
+    w = torch.tensor(W, dtype=g.dtype, device=g.device)
+    rho = g.sum(0)
+    j = torch.einsum('aq,qxyz->axyz', C, g)
+    Pi = torch.einsum('aq,bq,qxyz->abxyz', C, C, g)
+    ab = a[:, None, None, None]
+    s = j + 0.5 * rho * ab
+    u = s / rho
+    c2 = 1 - 0.5 * we
+    eye = torch.eye(3, dtype=g.dtype, device=g.device)
+    H0 = rho
+    H1 = j + rho * ab
+    H2 = (1 - we) * (Pi - eye[:, :, None, None, None] * rho / 3) + we * torch.einsum('axyz,bxyz->abxyz', s, s) / rho \
+        + c2 * (torch.einsum('a,bxyz->abxyz', a, s) + torch.einsum('b,axyz->abxyz', a, s))
+    cc = torch.einsum('aq,bq->abq', C, C) - eye[:, :, None] / 3
+    f = w[:, None, None, None] * (H0[None] + 3 * torch.einsum('aq,axyz->qxyz', C, H1)
+                                  + 4.5 * torch.einsum('abq,abxyz->qxyz', cc, H2))
+    return f, rho, u
+
+
 def run(phase, tau, g, uin, steps, magic=None, scheme='TRT', rho_out=1.0, periodic=(False, False, True)):
     """Returns the stored velocity of the last step, (3, nx, ny, nz)."""
     solid = solid_source(phase, periodic)
@@ -125,6 +148,6 @@ def run(phase, tau, g, uin, steps, magic=None, scheme='TRT', rho_out=1.0, period
     for _ in range(steps):
         gs = stream(f, solid)
         gs = apply_zou_he(gs, uin, rho_out)
-        f, rho, u = collide(gs, g, we, wo)
+        f, rho, u = collide_reg(gs, g, we) if scheme == 'REG' else collide(gs, g, we, wo)
         f = torch.where(fluid[None], f, w[:, None, None, None].expand_as(f))
     return u
