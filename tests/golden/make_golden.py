@@ -53,7 +53,7 @@ def spheres(shape, radius, porosity, rng):
 
 def cases():
     out = []
-    # BASELINE config 1 at the parity horizon
+    # the 4x34x4 gravity channel with solid rows, at 1000 steps
     nx, ny, nz = 4, 34, 4
     ph = np.ones((nx, ny, nz), np.uint8); ph[:, 0, :] = 0; ph[:, -1, :] = 0
     out.append(dict(name="c1_poiseuille", lat=[nx, ny, nz], scheme=BGK, kvisc=(0.8 - 0.5) / 3.0,
