@@ -56,7 +56,7 @@ def cases():
     # the 4x34x4 gravity channel with solid rows, at 1000 steps
     nx, ny, nz = 4, 34, 4
     ph = np.ones((nx, ny, nz), np.uint8); ph[:, 0, :] = 0; ph[:, -1, :] = 0
-    out.append(dict(name="c1_poiseuille", lat=[nx, ny, nz], scheme=BGK, kvisc=(0.8 - 0.5) / 3.0,
+    out.append(dict(name="poiseuille_4x34x4", lat=[nx, ny, nz], scheme=BGK, kvisc=(0.8 - 0.5) / 3.0,
                     g=[1e-6, 0, 0], bc=[PER] * 6, phase=ph, den=np.ones(ph.shape),
                     vel=np.zeros(ph.shape + (3,)), acc=None, chunks=[1000]))
     # lid-driven cavity, TRT, Zou-He lid on Y1

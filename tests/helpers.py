@@ -8,7 +8,7 @@ import os
 import numpy as np
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-CASES = ["c1_poiseuille", "cavity_trt", "porous_reg", "pdiff_sym", "couette_ladd",
+CASES = ["poiseuille_4x34x4", "cavity_trt", "porous_reg", "pdiff_sym", "couette_ladd",
          "random_mix_trt", "random_sym_reg", "z1_fixed_vel", "invel_grav",
          "edge_single_site", "edge_column_sym", "edge_sheet_zou_he", "edge_enclosed_site"]
 

@@ -20,7 +20,7 @@ def test_oracle_matches_reference_bitwise(name):
 
 
 def test_oracle_conserves_mass_periodic():
-    c = load_case("c1_poiseuille")
+    c = load_case("poiseuille_4x34x4")
     nf, f, den, vel = run_oracle(c, chunks=[200])
     fl = c["phase"] != 0
     assert abs(den[fl].sum() - nf) < 1e-10

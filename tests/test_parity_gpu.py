@@ -191,8 +191,8 @@ def test_acc_and_gravity_updates_between_calls():
     np.testing.assert_array_equal(np.asarray(s.get_den())[fl], o.get_den()[fl])
 
 
-def test_c1_chunking_is_irrelevant_without_zou_he():
-    c = load_case("c1_poiseuille")
+def test_chunking_is_irrelevant_without_zou_he():
+    c = load_case("poiseuille_4x34x4")
     _, f_a, _, v_a = run_engine(c, chunks=[1000])
     _, f_b, _, v_b = run_engine(c, chunks=[100] * 10)
     np.testing.assert_array_equal(f_a, f_b)
@@ -227,7 +227,7 @@ def test_reduce_matches_host_sums():
 
 
 @pytest.mark.parametrize("precision,tol", [(1, 2e-5), (2, 3e-2)])
-@pytest.mark.parametrize("name", ["c1_poiseuille", "cavity_trt", "porous_reg", "invel_grav"])
+@pytest.mark.parametrize("name", ["poiseuille_4x34x4", "cavity_trt", "porous_reg", "invel_grav"])
 def test_reduced_precision_velocity_error(name, precision, tol):
     # relative L2 velocity error of FP32-shifted (tol 2e-5) and FP16-storage
     # (tol 3e-2) against the FP64 reference outputs
