@@ -206,7 +206,8 @@ typedef struct jlb_domain {
     int32_t lat_size[3];  /* interior sites per axis                         */
     double kvisc;         /* kinematic viscosity                             */
     double g[3];          /* body force                                      */
-    int32_t bc[6];        /* JLB_WALL / JLB_PERIODIC per face                 */
+    int32_t bc[6];        /* JLB_WALL .. JLB_SYMMETRIC per face; Zou-He data
+                             come from den / vel at jlb_batch_create          */
     double trt_magic;     /* as in jlb_config                                */
     const uint8_t *phase; /* (nx,ny,nz) interior phase, k fastest, 0 = solid */
     const double *den;    /* (nx,ny,nz) initial density or NULL (1)          */

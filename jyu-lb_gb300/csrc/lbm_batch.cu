@@ -37,7 +37,7 @@ __global__ void __launch_bounds__(BLOCK, JLB_BATCH_WARPS * 32 / BLOCK)
     if (l >= D.n) return;
     const int32_t n = D.off + l;
     const uint8_t cls = __ldg(a.ncls + n);
-    if (cls == BCLS_SOLID) return;
+    if (cls >= BCLS_SOLID) return;
     // rows of 19 * Np exceed 2^31 elements for large ensembles; each row
     // itself is indexed by a 32-bit site
     const uint32_t m = (PSTEP && cls != BCLS_PLAIN) ? __ldg(a.nmask + n) : 0u;
@@ -142,6 +142,46 @@ int launch_batch_step(const BatchArgs &a, int scheme, bool pstep, int block, int
     return (int)cudaGetLastError();
 }
 
+// Boundary nodes: the single-domain boundary-node step with the relaxation
+// rates, body force and face kinds of each node's domain.
+template <int SCH, bool PSTEP>
+__global__ void __launch_bounds__(128) lbm_batch_special_kernel(const BatchArgs a) {
+    const int t = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    if (t >= a.Msp) return;
+    const BatchDomain &D = a.dom[__ldg(a.sp_dom + t)];
+    StepArgs s{};
+    s.f = a.f;
+    s.Np = a.Np;
+    s.M = a.Msp;
+    s.sp_node = a.sp_node;
+    s.sp_info = a.sp_info;
+    s.sp_rd = a.sp_rd;
+    s.sp_wr = a.sp_wr;
+    s.sp_lw = a.sp_lw;
+    s.sp_bc = a.sp_bc;
+    s.sp_den = a.sp_den;
+    s.den = a.den; s.ux = a.ux; s.uy = a.uy; s.uz = a.uz;
+    s.write_moments = a.write_moments;
+    s.w_e = D.we;
+    s.w_o = D.wo;
+    for (int c = 0; c < 3; ++c) s.g[c] = D.g[c];
+    for (int f = 0; f < 6; ++f) s.bc[f] = D.bc[f];
+    special_node<StoreF32, PhysSh<SCH>, PSTEP, false>(s, (int)blockIdx.x);
+}
+
+int launch_batch_special(const BatchArgs &a, int scheme, bool pstep, cudaStream_t st) {
+    if (a.Msp <= 0) return 0;
+    const unsigned blocks = (unsigned)((a.Msp + 127) / 128);
+#define JLB_BS2(SCH) \
+    if (pstep) lbm_batch_special_kernel<SCH, true><<<blocks, 128, 0, st>>>(a); \
+    else lbm_batch_special_kernel<SCH, false><<<blocks, 128, 0, st>>>(a);
+    if (scheme == SCH_BGK) { JLB_BS2(SCH_BGK) }
+    else if (scheme == SCH_TRT) { JLB_BS2(SCH_TRT) }
+    else { JLB_BS2(SCH_REG) }
+#undef JLB_BS2
+    return (int)cudaGetLastError();
+}
+
 // gathers one domain's initial populations (single-domain S_post layout,
 // stride Np_d) into the packed array (stride Np)
 __global__ void batch_pack_kernel(const float *src, int64_t Np_d, int32_t n_d, float *dst, int64_t Np,
@@ -188,8 +228,25 @@ __global__ void batch_readout_kernel(BatchArgs a, int d, int parity, double *out
     });
 }
 
-int launch_batch_readout(const BatchArgs &a, int d, int n_d, int parity, double *out, cudaStream_t st) {
+// boundary nodes [t0, t1) of domain d: their streamed slots come from the
+// tables (mirrors and Zou-He faces), overwriting what the kernel above wrote
+__global__ void batch_readout_special_kernel(BatchArgs a, int d, int t0, int t1, int parity, double *out) {
+    const int t = t0 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    if (t >= t1) return;
+    const BatchDomain &D = a.dom[d];
+    const int64_t n = a.sp_node[t];
+    const int64_t l = n - D.off;
+    Unroll<0, Q>::run([&]<int q>() {
+        constexpr double w = WCLASS(q) == 0 ? (12.0 / 36.0) : WCLASS(q) == 1 ? (2.0 / 36.0) : (1.0 / 36.0);
+        const int64_t e = parity == 0 ? (int64_t)OPP(q) * a.Np + n : a.sp_wr[(int64_t)q * a.Msp + t];
+        out[(int64_t)q * D.n + l] = (double)a.f[e] + w;
+    });
+}
+
+int launch_batch_readout(const BatchArgs &a, int d, int n_d, int parity, int t0, int t1, double *out,
+                         cudaStream_t st) {
     batch_readout_kernel<<<(n_d + 255) / 256, 256, 0, st>>>(a, d, parity, out);
+    if (t1 > t0) batch_readout_special_kernel<<<(t1 - t0 + 127) / 128, 128, 0, st>>>(a, d, t0, t1, parity, out);
     return (int)cudaGetLastError();
 }
 

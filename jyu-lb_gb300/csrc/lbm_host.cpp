@@ -1561,6 +1561,15 @@ struct jlb_batch {
     double tune_ms[3] = {0, 0, 0}; // per-step time of blocks 64 / 128 / 256
     cudaGraphExec_t gexec[2] = {nullptr, nullptr};
     int GK = 32;
+    // boundary nodes of domains with Zou-He or symmetric faces (device
+    // tables in the single-domain layout, element indices into f)
+    int Msp = 0;
+    std::vector<int> sp_first;    // [ndom + 1]: domain d owns boundary nodes [sp_first[d], sp_first[d+1])
+    int32_t *d_sp_dom = nullptr;
+    int64_t *d_sp_node = nullptr, *d_sp_rd = nullptr, *d_sp_wr = nullptr;
+    uint32_t *d_sp_info = nullptr;
+    double *d_sp_lw = nullptr, *d_sp_bc = nullptr;
+    float *d_sp_den = nullptr;
     std::string err;
 };
 
@@ -1593,6 +1602,12 @@ BatchArgs batch_args(const jlb_batch *b, int write_moments) {
     a.dprev = b->dprev;
     a.den = b->mom[0]; a.ux = b->mom[1]; a.uy = b->mom[2]; a.uz = b->mom[3];
     a.write_moments = write_moments;
+    a.Msp = b->Msp;
+    a.sp_dom = b->d_sp_dom;
+    a.sp_node = b->d_sp_node; a.sp_rd = b->d_sp_rd; a.sp_wr = b->d_sp_wr;
+    a.sp_info = b->d_sp_info;
+    a.sp_lw = b->d_sp_lw; a.sp_bc = b->d_sp_bc;
+    a.sp_den = b->d_sp_den;
     return a;
 }
 
@@ -1621,9 +1636,15 @@ int batch_tiles(jlb_batch *b, int block) {
 }
 
 int batch_launch(jlb_batch *b, bool pstep, int write_moments) {
-    const int r = launch_batch_step(batch_args(b, write_moments), b->scheme, pstep, b->block, b->ntiles, b->st);
+    const BatchArgs a = batch_args(b, write_moments);
+    int r = launch_batch_step(a, b->scheme, pstep, b->block, b->ntiles, b->st);
     if (r) return bfail(b, JLB_ERR_CUDA, std::string("batch step: ") + cudaGetErrorString((cudaError_t)r));
     ++b->launches;
+    if (b->Msp > 0) {
+        r = launch_batch_special(a, b->scheme, pstep, b->st);
+        if (r) return bfail(b, JLB_ERR_CUDA, std::string("batch boundary nodes: ") + cudaGetErrorString((cudaError_t)r));
+        ++b->launches;
+    }
     return JLB_OK;
 }
 
@@ -1642,13 +1663,13 @@ int batch_run(jlb_batch *b, uint32_t n, bool write_last) {
             cudaError_t ce = cudaStreamEndCapture(b->st, &g);
             if (rr) return rr;
             if (ce != cudaSuccess) return bfail(b, JLB_ERR_CUDA, "batch graph capture failed");
-            b->launches -= b->GK;
+            b->launches -= (uint64_t)b->GK * (1 + (b->Msp > 0));
             ce = cudaGraphInstantiate(&b->gexec[p], g, 0);
             cudaGraphDestroy(g);
             if (ce != cudaSuccess) return bfail(b, JLB_ERR_CUDA, "batch graph instantiate failed");
         }
         BCK(cudaGraphLaunch(b->gexec[p], b->st));
-        b->launches += b->GK;
+        b->launches += (uint64_t)b->GK * (1 + (b->Msp > 0));
         plain -= b->GK;
         if (b->GK & 1) b->parity ^= 1;
     }
@@ -1677,6 +1698,9 @@ int batch_autotune(jlb_batch *b) {
     }
     BCK(cudaMemcpyAsync(fsave, b->f, fb, cudaMemcpyDeviceToDevice, b->st));
     BCK(cudaMemcpyAsync(dsave, b->dprev, db, cudaMemcpyDeviceToDevice, b->st));
+    std::vector<float> spsave((size_t)b->Msp);
+    if (b->Msp > 0)
+        BCK(cudaMemcpyAsync(spsave.data(), b->d_sp_den, spsave.size() * sizeof(float), cudaMemcpyDeviceToHost, b->st));
     const int cand[3] = {64, 128, 256};
     int best = 128;
     double best_ms = 1e30;
@@ -1698,9 +1722,11 @@ int batch_autotune(jlb_batch *b) {
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    b->launches -= 18; // tuning steps are not part of the run
+    b->launches -= 18 * (1 + (b->Msp > 0)); // tuning steps are not part of the run
     BCK(cudaMemcpyAsync(b->f, fsave, fb, cudaMemcpyDeviceToDevice, b->st));
     BCK(cudaMemcpyAsync(b->dprev, dsave, db, cudaMemcpyDeviceToDevice, b->st));
+    if (b->Msp > 0)
+        BCK(cudaMemcpyAsync(b->d_sp_den, spsave.data(), spsave.size() * sizeof(float), cudaMemcpyHostToDevice, b->st));
     BCK(cudaStreamSynchronize(b->st));
     cudaFree(fsave);
     cudaFree(dsave);
@@ -1717,7 +1743,8 @@ void jlb_batch_destroy(jlb_batch *b) {
     for (int p = 0; p < 2; ++p)
         if (b->gexec[p]) cudaGraphExecDestroy(b->gexec[p]);
     void *bufs[] = {b->f, b->dprev, b->mom[0], b->mom[1], b->mom[2], b->mom[3], b->ncls, b->nmask, b->mmask,
-                    b->d_dom, b->tile_dom};
+                    b->d_dom, b->tile_dom, b->d_sp_dom, b->d_sp_node, b->d_sp_rd, b->d_sp_wr, b->d_sp_info,
+                    b->d_sp_lw, b->d_sp_bc, b->d_sp_den};
     for (void *p : bufs)
         if (p) cudaFree(p);
     if (b->own_stream && b->st) cudaStreamDestroy(b->st);
@@ -1764,11 +1791,7 @@ int jlb_batch_create(int32_t scheme, const jlb_domain *doms, int32_t ndom, void 
             b->err = "domain " + std::to_string(d) + ": " + msg;
             return bail(JLB_ERR_INVALID_ARG);
         }
-        for (int f = 0; f < 6; ++f)
-            if (D.bc[f] != JLB_WALL && D.bc[f] != JLB_PERIODIC) {
-                b->err = "domain " + std::to_string(d) + ": batched domains support WALL and PERIODIC faces";
-                return bail(JLB_ERR_UNSUPPORTED);
-            }
+
         if (!D.phase) { b->err = "domain " + std::to_string(d) + ": phase is NULL"; return bail(JLB_ERR_INVALID_ARG); }
         BatchDomain &B = b->dom[d];
         B.nx = D.lat_size[0]; B.ny = D.lat_size[1]; B.nz = D.lat_size[2];
@@ -1778,6 +1801,7 @@ int jlb_batch_create(int32_t scheme, const jlb_domain *doms, int32_t ndom, void 
         B.n = (int32_t)n;
         B.inv_syz = 1.0f / (float)(B.ny * B.nz);
         B.inv_nz = 1.0f / (float)B.nz;
+        for (int f = 0; f < 6; ++f) B.bc[f] = D.bc[f];
         off += ((n + 127) / 128) * 128;
         const double tau_e = 0.5 + 3.0 * D.kvisc;
         const double we = 1.0 / tau_e;
@@ -1814,6 +1838,16 @@ int jlb_batch_create(int32_t scheme, const jlb_domain *doms, int32_t ndom, void 
     std::vector<uint32_t> mm, lm;
     std::vector<float> dp;
     b->nfluid_dom.assign(ndom, 0);
+    // boundary nodes of domains with Zou-He or symmetric faces, per node:
+    // domain, packed node, info, 19 read / write elements, 19 c.u_wall, 2 x 4
+    // Zou-He values, previous density
+    std::vector<int32_t> g_dom;
+    std::vector<int64_t> g_node;
+    std::vector<uint32_t> g_info;
+    std::vector<int64_t> g_rd, g_wr;   // node-major [t][19] until the upload
+    std::vector<double> g_lw, g_bc;    // [t][19], [t][8]
+    std::vector<float> g_den;
+    b->sp_first.assign(ndom + 1, 0);
     for (int d = 0; d < ndom; ++d) {
         const jlb_domain &D = doms[d];
         BatchDomain &B = b->dom[d];
@@ -1850,6 +1884,34 @@ int jlb_batch_create(int32_t scheme, const jlb_domain *doms, int32_t ndom, void 
             r = launch_batch_pack((const float *)s->f, s->Np, B.n, b->f, b->Np, B.off, b->st);
             if (r) { b->err = "pack kernel failed"; jlb_destroy(s); return bail(JLB_ERR_CUDA); }
         }
+        // boundary nodes of a domain with Zou-He or symmetric faces take the
+        // table path (with their moving-wall links); the tables translate the
+        // single-domain element indices q * Np_d + m into the packed array
+        bool routed = false;
+        for (int f = 0; f < 6; ++f)
+            routed |= D.bc[f] == JLB_FIXED_DEN || D.bc[f] == JLB_FIXED_VEL || D.bc[f] == JLB_SYMMETRIC;
+        b->sp_first[d] = (int)g_node.size();
+        if (routed && nf > 0 && s->M > 0) {
+            const int M = s->M;
+            std::vector<double> bcbuf((size_t)8 * M, 0.0);
+            std::vector<float> denbuf((size_t)M, 0.0f);
+            fill_dynamic(s, den.data(), vel.data(), bcbuf.data(), denbuf.data());
+            const int64_t Npd = s->Np;
+            auto tr = [&](int64_t e) { return (e / Npd) * b->Np + B.off + (e % Npd); };
+            for (int t = 0; t < M; ++t) {
+                g_dom.push_back(d);
+                g_node.push_back(B.off + s->sp_node[t]);
+                g_info.push_back(s->sp_info[t]);
+                for (int q = 0; q < 19; ++q) {
+                    g_rd.push_back(tr(s->sp_rd[(size_t)q * M + t]));
+                    g_wr.push_back(tr(s->sp_wr[(size_t)q * M + t]));
+                    g_lw.push_back(s->sp_lw[(size_t)q * M + t]);
+                }
+                for (int c = 0; c < 8; ++c) g_bc.push_back(c < 4 * s->bc_slots ? bcbuf[(size_t)c * M + t] : 0.0);
+                g_den.push_back(denbuf[t]);
+            }
+        }
+        b->sp_first[d + 1] = (int)g_node.size();
         // node classes and masks; the moving solids of a domain share one velocity
         cls.assign(B.n, BCLS_SOLID);
         lm.assign(B.n, 0);
@@ -1861,6 +1923,11 @@ int jlb_batch_create(int32_t scheme, const jlb_domain *doms, int32_t ndom, void 
             const uint32_t m = s->hmask[l];
             if (m & MASK_SOLID) continue;
             const int i = (int)(l / ((int64_t)B.ny * B.nz)), j = (int)((l / B.nz) % B.ny), k = (int)(l % B.nz);
+            if (routed && (m & MASK_SPECIAL)) {
+                lm[l] = m & MASK_LINKS;
+                cls[l] = BCLS_SPECIAL;
+                continue;
+            }
             uint32_t mv = 0;
             for (int q = 0; q < 19; ++q) {
                 if (!(m & (1u << q))) continue;
@@ -1889,6 +1956,39 @@ int jlb_batch_create(int32_t scheme, const jlb_domain *doms, int32_t ndom, void 
         cudaError_t e5 = cudaStreamSynchronize(b->st); // host vectors are reused next domain
         jlb_destroy(s);
         if (e1 || e2 || e3 || e4 || e5) { b->err = "domain upload failed"; return bail(JLB_ERR_CUDA); }
+    }
+    b->Msp = (int)g_node.size();
+    if (b->Msp > 0) {
+        const int M = b->Msp;
+        // node-major [t][19] -> [19][M] as the boundary-node path reads them
+        std::vector<int64_t> rd((size_t)19 * M), wr((size_t)19 * M);
+        std::vector<double> lw((size_t)19 * M), bcd((size_t)8 * M);
+        for (int t = 0; t < M; ++t) {
+            for (int q = 0; q < 19; ++q) {
+                rd[(size_t)q * M + t] = g_rd[(size_t)t * 19 + q];
+                wr[(size_t)q * M + t] = g_wr[(size_t)t * 19 + q];
+                lw[(size_t)q * M + t] = g_lw[(size_t)t * 19 + q];
+            }
+            for (int c = 0; c < 8; ++c) bcd[(size_t)c * M + t] = g_bc[(size_t)t * 8 + c];
+        }
+        if ((r = alloc((void **)&b->d_sp_dom, (size_t)M * 4)) || (r = alloc((void **)&b->d_sp_node, (size_t)M * 8)) ||
+            (r = alloc((void **)&b->d_sp_info, (size_t)M * 4)) || (r = alloc((void **)&b->d_sp_rd, rd.size() * 8)) ||
+            (r = alloc((void **)&b->d_sp_wr, wr.size() * 8)) || (r = alloc((void **)&b->d_sp_lw, lw.size() * 8)) ||
+            (r = alloc((void **)&b->d_sp_bc, bcd.size() * 8)) || (r = alloc((void **)&b->d_sp_den, (size_t)M * 4)))
+            return bail(r);
+        cudaError_t e = cudaSuccess;
+        auto up = [&](void *dst, const void *src, size_t n) {
+            if (e == cudaSuccess) e = cudaMemcpy(dst, src, n, cudaMemcpyHostToDevice);
+        };
+        up(b->d_sp_dom, g_dom.data(), (size_t)M * 4);
+        up(b->d_sp_node, g_node.data(), (size_t)M * 8);
+        up(b->d_sp_info, g_info.data(), (size_t)M * 4);
+        up(b->d_sp_rd, rd.data(), rd.size() * 8);
+        up(b->d_sp_wr, wr.data(), wr.size() * 8);
+        up(b->d_sp_lw, lw.data(), lw.size() * 8);
+        up(b->d_sp_bc, bcd.data(), bcd.size() * 8);
+        up(b->d_sp_den, g_den.data(), (size_t)M * 4);
+        if (e != cudaSuccess) { b->err = "boundary-node table upload failed"; return bail(JLB_ERR_CUDA); }
     }
     const char *tune = std::getenv("JLB_BATCH_BLOCK");
     if (tune && tune[0]) r = batch_tiles(b, std::atoi(tune));
@@ -1929,7 +2029,8 @@ int jlb_batch_populations(jlb_batch *b, int32_t d, double *f) {
     const BatchDomain &B = b->dom[d];
     double *tmp = nullptr;
     BCK(cudaMalloc(&tmp, (size_t)19 * B.n * sizeof(double)));
-    int r = launch_batch_readout(batch_args(b, 0), d, B.n, b->parity, tmp, b->st);
+    int r = launch_batch_readout(batch_args(b, 0), d, B.n, b->parity, b->sp_first[d], b->sp_first[d + 1], tmp,
+                                 b->st);
     cudaError_t e = r ? (cudaError_t)r
                       : cudaMemcpyAsync(f, tmp, (size_t)19 * B.n * sizeof(double), cudaMemcpyDeviceToHost, b->st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(b->st);

@@ -69,9 +69,81 @@ def test_ensemble_matches_single_domain_runs(scheme, steps):
         assert abs(den[fl] - np.asarray(s64.get_den())[fl]).max() <= 1e-6
 
 
-def test_ensemble_rejects_unsupported_faces():
+def test_ensemble_rejects_unsupported_setups():
     from jyulb.ensemble import Domain, Ensemble
 
-    ph = np.ones((4, 4, 4), np.uint8)
-    with pytest.raises(RuntimeError, match="WALL and PERIODIC"):
-        Ensemble([Domain(ph, bc=[3, 2, 1, 1, 1, 1])], 0)
+    # moving solids of a domain without Zou-He / symmetric faces share one
+    # velocity (the in-kernel Ladd term)
+    ph = np.ones((6, 6, 4), np.uint8)
+    ph[:, 0, :] = 0
+    ph[:, -1, :] = 0
+    vel = np.zeros((6, 6, 4, 3))
+    vel[:, 0, :, 0] = 0.01
+    vel[:, -1, :, 0] = 0.02
+    with pytest.raises(RuntimeError, match="share one velocity"):
+        Ensemble([Domain(ph, vel=vel)], 0)
+    # the single-domain checks apply: fixed faces only on opposite pairs
+    with pytest.raises(ValueError):
+        Ensemble([Domain(np.ones((4, 4, 4), np.uint8), bc=[3, 1, 2, 1, 1, 1])], 0)
+
+
+def _boundary_domains(seed):
+    # uneven boundary sets: Zou-He velocity inlet / density outlet, Zou-He
+    # pressure difference, symmetric faces, moving solids next to Zou-He
+    # faces, and a plain channel with a moving top wall
+    from jyulb.defs import FIXED_DEN, FIXED_VEL, PERIODIC, SYMMETRIC, WALL
+
+    rng = np.random.default_rng(seed)
+    out = []
+    sh = (14, 9, 6)
+    ph = np.ones(sh, np.uint8); ph[6:8, 3:6, :] = 0
+    vel = np.zeros(sh + (3,)); vel[0, :, :, 0] = 0.02
+    out.append(dict(phase=ph, den=None, vel=vel, kvisc=0.05, g=[0.0, 0.0, 0.0],
+                    bc=[FIXED_VEL, FIXED_DEN, WALL, WALL, PERIODIC, PERIODIC]))
+    sh = (12, 7, 5)
+    den = np.ones(sh); den[0] = 1.01; den[-1] = 0.99
+    out.append(dict(phase=np.ones(sh, np.uint8), den=den, vel=None, kvisc=0.08, g=[0.0, 0.0, 0.0],
+                    bc=[FIXED_DEN, FIXED_DEN, WALL, SYMMETRIC, PERIODIC, PERIODIC]))
+    sh = (8, 10, 7)
+    out.append(dict(phase=np.ones(sh, np.uint8), den=None, vel=None, kvisc=0.04, g=[0.0, 0.0, 2e-5],
+                    bc=[SYMMETRIC, WALL, SYMMETRIC, SYMMETRIC, PERIODIC, PERIODIC]))
+    sh = (10, 8, 6)
+    ph = np.ones(sh, np.uint8); ph[:, -1, :] = 0
+    vel = np.zeros(sh + (3,)); vel[:, -1, :, 2] = 0.03; vel[0, :-1, :, 0] = 0.01
+    out.append(dict(phase=ph, den=None, vel=vel, kvisc=0.06, g=[1e-5, 0.0, 0.0],
+                    bc=[FIXED_VEL, FIXED_DEN, WALL, WALL, PERIODIC, PERIODIC]))
+    sh = (9, 8, 5)
+    ph = np.ones(sh, np.uint8); ph[:, 0, :] = 0; ph[:, -1, :] = 0
+    vel = np.zeros(sh + (3,)); vel[:, -1, :, 0] = 0.02
+    out.append(dict(phase=ph, den=None, vel=vel, kvisc=0.1, g=[float(rng.uniform(1e-6, 1e-5)), 0.0, 0.0],
+                    bc=[PERIODIC] * 6))
+    return out
+
+
+@pytest.mark.parametrize("scheme", [0, 1, 2])
+def test_ensemble_boundary_sets_match_single_domains(scheme):
+    from jyulb.ensemble import Domain, Ensemble
+    from jyulb.isothermal import Solver
+
+    cs = _boundary_domains(7)
+    ens = Ensemble([Domain(c["phase"], c["den"], c["vel"], c["kvisc"], c["g"], c["bc"]) for c in cs], scheme)
+    steps = 37
+    ens.evolve(steps)
+    for d, c in enumerate(cs):
+        s = Solver(np.array(c["phase"].shape, dtype=np.int32), scheme, c["kvisc"], np.array(c["g"]),
+                   np.array(c["bc"], dtype=np.int32), precision=1)
+        s.get_phase()[:] = c["phase"]
+        if c["den"] is not None:
+            s.get_den()[:] = c["den"]
+        if c["vel"] is not None:
+            s.get_vel()[:] = c["vel"]
+        s.finalize_init()
+        s.evolve(steps)  # one call: boundary data read once, as the ensemble does
+        fl = c["phase"] != 0
+        den, vel = ens.moments(d)
+        v32 = np.asarray(s.get_vel())
+        vmax = np.abs(v32[fl]).max()
+        assert np.abs(vel[fl] - v32[fl]).max() <= 1e-5 * vmax + 1e-12, d
+        assert np.abs(den[fl] - np.asarray(s.get_den())[fl]).max() <= 1e-6, d
+        f = ens.populations(d)
+        assert np.abs(f[:, fl] - s.populations()[:, fl]).max() <= 1e-7, d
