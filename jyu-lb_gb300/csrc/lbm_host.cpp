@@ -1890,6 +1890,18 @@ int jlb_batch_create(int32_t scheme, const jlb_domain *doms, int32_t ndom, void 
         bool routed = false;
         for (int f = 0; f < 6; ++f)
             routed |= D.bc[f] == JLB_FIXED_DEN || D.bc[f] == JLB_FIXED_VEL || D.bc[f] == JLB_SYMMETRIC;
+        // so do domains whose moving solids have more than one velocity (the
+        // packed kernel's Ladd term takes one velocity per domain)
+        if (!routed && D.vel) {
+            const double *v0 = nullptr;
+            for (int64_t l = 0; l < B.n && !routed; ++l) {
+                if (D.phase[l] != 0) continue;
+                const double *u = D.vel + 3 * l;
+                if (u[0] == 0.0 && u[1] == 0.0 && u[2] == 0.0) continue;
+                if (!v0) v0 = u;
+                else routed = u[0] != v0[0] || u[1] != v0[1] || u[2] != v0[2];
+            }
+        }
         b->sp_first[d] = (int)g_node.size();
         if (routed && nf > 0 && s->M > 0) {
             const int M = s->M;

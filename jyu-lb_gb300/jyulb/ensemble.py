@@ -12,10 +12,10 @@ Each domain is described like a Solver: interior ``phase``, ``den`` and
 (WALL, PERIODIC, FIXED_DEN, FIXED_VEL or SYMMETRIC).  ``vel`` on solid sites
 gives moving walls (Ladd's term).  Zou-He faces take their data from ``den``
 and ``vel`` once, at set-up (a Solver re-reads them at every evolve call).
-The boundary nodes of domains with Zou-He or symmetric faces run the
-single-domain boundary-node path in a second launch per step.  In the other
-domains all moving solids must share one velocity.  The relaxation scheme
-is common to the ensemble.
+The boundary nodes of domains with Zou-He or symmetric faces, or with
+moving solids of more than one velocity, run the single-domain
+boundary-node path in a second launch per step.  The relaxation scheme is
+common to the ensemble.
 """
 from __future__ import annotations
 

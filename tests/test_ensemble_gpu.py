@@ -69,19 +69,9 @@ def test_ensemble_matches_single_domain_runs(scheme, steps):
         assert abs(den[fl] - np.asarray(s64.get_den())[fl]).max() <= 1e-6
 
 
-def test_ensemble_rejects_unsupported_setups():
+def test_ensemble_rejects_invalid_boundary_sets():
     from jyulb.ensemble import Domain, Ensemble
 
-    # moving solids of a domain without Zou-He / symmetric faces share one
-    # velocity (the in-kernel Ladd term)
-    ph = np.ones((6, 6, 4), np.uint8)
-    ph[:, 0, :] = 0
-    ph[:, -1, :] = 0
-    vel = np.zeros((6, 6, 4, 3))
-    vel[:, 0, :, 0] = 0.01
-    vel[:, -1, :, 0] = 0.02
-    with pytest.raises(RuntimeError, match="share one velocity"):
-        Ensemble([Domain(ph, vel=vel)], 0)
     # the single-domain checks apply: fixed faces only on opposite pairs
     with pytest.raises(ValueError):
         Ensemble([Domain(np.ones((4, 4, 4), np.uint8), bc=[3, 1, 2, 1, 1, 1])], 0)
@@ -117,6 +107,12 @@ def _boundary_domains(seed):
     vel = np.zeros(sh + (3,)); vel[:, -1, :, 0] = 0.02
     out.append(dict(phase=ph, den=None, vel=vel, kvisc=0.1, g=[float(rng.uniform(1e-6, 1e-5)), 0.0, 0.0],
                     bc=[PERIODIC] * 6))
+    # two plates moving at different velocities (Couette): the boundary-node
+    # path, as no single wall velocity serves the domain
+    sh = (10, 6, 4)
+    ph = np.ones(sh, np.uint8); ph[0] = 0; ph[-1] = 0
+    vel = np.zeros(sh + (3,)); vel[0, :, :, 1] = -0.01; vel[-1, :, :, 1] = 0.015; vel[-1, :, :, 2] = 0.005
+    out.append(dict(phase=ph, den=None, vel=vel, kvisc=0.07, g=[0.0, 0.0, 0.0], bc=[PERIODIC] * 6))
     return out
 
 
