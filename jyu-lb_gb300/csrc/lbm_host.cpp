@@ -2174,9 +2174,6 @@ int jlb_adj_create(const jlb_config *cfg, const uint8_t *phase, int32_t loss_pla
     for (int f = 1; f < 6; ++f)
         if (cfg->bc[f] == JLB_FIXED_VEL)
             return afail(nullptr, JLB_ERR_UNSUPPORTED, "adjoint: FIXED_VEL is supported on face 1X only");
-    for (int f = 0; f < 6; ++f)
-        if (cfg->bc[f] == JLB_SYMMETRIC)
-            return afail(nullptr, JLB_ERR_UNSUPPORTED, "adjoint: SYMMETRIC faces are not supported");
     if (cfg->bc[0] == JLB_FIXED_VEL && cfg->bc[1] != JLB_PERIODIC && cfg->lat_size[0] == 1)
         return afail(nullptr, JLB_ERR_UNSUPPORTED, "adjoint: a one-site-thick domain with two Zou-He faces");
     if (loss_plane < 0 || loss_plane >= cfg->lat_size[0]) return afail(nullptr, JLB_ERR_INVALID_ARG, "loss plane out of range");

@@ -25,7 +25,7 @@ def setup(seed=0, shape=(16, 10, 6), r=2.0):
     return phase, uin, target
 
 
-def torch_grads(phase, tau, g, uin, target, steps, plane, scheme, magic, zwall=False):
+def torch_grads(phase, tau, g, uin, target, steps, plane, scheme, magic, zwall=False, zsym=False):
     import torch
 
     from torch_lbm import run
@@ -33,7 +33,8 @@ def torch_grads(phase, tau, g, uin, target, steps, plane, scheme, magic, zwall=F
     t_tau = torch.tensor(tau, dtype=torch.float64, requires_grad=True)
     t_g = torch.tensor(g, dtype=torch.float64, requires_grad=True)
     t_uin = torch.tensor(uin, dtype=torch.float64, requires_grad=True)
-    u = run(phase, t_tau, t_g, t_uin, steps, magic=magic, scheme=scheme, periodic=(False, False, not zwall))
+    u = run(phase, t_tau, t_g, t_uin, steps, magic=magic, scheme=scheme, periodic=(False, False, not zwall),
+            zsym=zsym)
     fl = torch.from_numpy(phase[plane] != 0)
     d = u[:, plane].permute(1, 2, 0) - torch.tensor(target)
     L = (d[fl] ** 2).sum()
@@ -41,25 +42,28 @@ def torch_grads(phase, tau, g, uin, target, steps, plane, scheme, magic, zwall=F
     return float(L.detach()), float(t_tau.grad), t_g.grad.numpy(), t_uin.grad.numpy()
 
 
-@pytest.mark.parametrize("scheme,zwall", [("TRT", False), ("BGK", False), ("TRT", True), ("REG", False),
-                                          ("REG", True)])
-def test_fp64_adjoint_matches_torch_autograd(scheme, zwall):
+@pytest.mark.parametrize("scheme,zb_name", [("TRT", "periodic"), ("BGK", "periodic"), ("TRT", "wall"),
+                                            ("REG", "periodic"), ("REG", "wall"), ("TRT", "symmetric"),
+                                            ("REG", "symmetric")])
+def test_fp64_adjoint_matches_torch_autograd(scheme, zb_name):
     from jyulb.adjoint import ChannelProblem
-    from jyulb.defs import BGK, FIXED_DEN, FIXED_VEL, FP64, PERIODIC, REGULARIZATION, TRT, WALL
+    from jyulb.defs import BGK, FIXED_DEN, FIXED_VEL, FP64, PERIODIC, REGULARIZATION, SYMMETRIC, TRT, WALL
 
+    zwall, zsym = zb_name == "wall", zb_name == "symmetric"
     phase, uin, target = setup(1)
-    tau, g, steps, plane = 0.8, np.array([1e-5, 2e-6, 1e-6 if zwall else 0.0]), 30, 12
+    tau, g, steps, plane = 0.8, np.array([1e-5, 2e-6, 1e-6 if (zwall or zsym) else 0.0]), 30, 12
     magic = 0.25 if scheme == "TRT" else None
-    zb = WALL if zwall else PERIODIC
+    zb = WALL if zwall else SYMMETRIC if zsym else PERIODIC
     sch = {"TRT": TRT, "BGK": BGK, "REG": REGULARIZATION}[scheme]
     p = ChannelProblem(phase, bc=[FIXED_VEL, FIXED_DEN, WALL, WALL, zb, zb], rlx_scheme=sch,
                        precision=FP64, trt_magic=magic, loss_plane=plane, checkpoint_every=7)
     L, _ = p.forward(tau, g, uin, steps, target)
     dtau, dg, duin = p.backward()
-    Lt, dtau_t, dg_t, duin_t = torch_grads(phase, tau, g, uin, target, steps, plane, scheme, magic, zwall)
+    Lt, dtau_t, dg_t, duin_t = torch_grads(phase, tau, g, uin, target, steps, plane, scheme, magic, zwall, zsym)
     assert abs(L - Lt) <= 1e-10 * abs(Lt)
     assert abs(dtau - dtau_t) <= 1e-8 * abs(dtau_t)
-    np.testing.assert_allclose(dg[:3 if zwall else 2], dg_t[:3 if zwall else 2], rtol=1e-8)
+    nd = 3 if (zwall or zsym) else 2
+    np.testing.assert_allclose(dg[:nd], dg_t[:nd], rtol=1e-8)
     np.testing.assert_allclose(duin, duin_t, rtol=1e-7, atol=1e-9 * np.abs(duin_t).max())
 
 

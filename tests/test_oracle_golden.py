@@ -57,11 +57,13 @@ def test_oracle_steady_profiles_match_reference():
         assert pc.error(prof, c, flow_field) == float.fromhex(gold[c["name"]]["error"])
 
 
+@pytest.mark.parametrize("zsym", [False, True])
 @pytest.mark.parametrize("scheme", ["BGK", "TRT", "REG"])
-def test_torch_step_matches_oracle(scheme):
+def test_torch_step_matches_oracle(scheme, zsym):
     # the pure-torch FP64 step that checks the adjoint's gradients reproduces
     # the oracle (and so the reference) on its channel: Zou-He velocity inlet
-    # with a per-site u_x, density outlet, walls in y, periodic z, a cylinder
+    # with a per-site u_x, density outlet, walls in y, periodic or symmetric z,
+    # a cylinder
     import torch
 
     from pyoracle import Oracle
@@ -75,9 +77,11 @@ def test_torch_step_matches_oracle(scheme):
     uin = 0.02 + 0.005 * rng.standard_normal((ny, nz))
     tau, g, steps = 0.8, np.array([1e-5, 2e-6, 0.0]), 25
     sch = {"BGK": 0, "TRT": 1, "REG": 2}[scheme]
+    if zsym:
+        g = np.array([1e-5, 2e-6, 3e-6])
     u = run(phase, torch.tensor(tau, dtype=torch.float64), torch.tensor(g), torch.tensor(uin), steps,
-            scheme=scheme).numpy()
-    o = Oracle([nx, ny, nz], sch, (tau - 0.5) / 3.0, list(g), [3, 2, 0, 0, 1, 1])
+            scheme=scheme, zsym=zsym).numpy()
+    o = Oracle([nx, ny, nz], sch, (tau - 0.5) / 3.0, list(g), [3, 2, 0, 0, 4, 4] if zsym else [3, 2, 0, 0, 1, 1])
     o.get_phase()[:] = phase
     o.finalize_init()  # from rest, as the torch step starts
     o.get_vel()[0, :, :, 0] = uin  # inlet data, read at the evolve call

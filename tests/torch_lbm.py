@@ -19,9 +19,10 @@ NNZ = [abs(a) + abs(b) + abs(c) for a, b, c in zip(CI, CJ, CK)]
 W = [1 / 3 if n == 0 else (1 / 18 if n == 1 else 1 / 36) for n in NNZ]
 
 
-def solid_source(phase, periodic):
+def solid_source(phase, periodic, zsym=False):
     """(19, nx, ny, nz) bool: the upstream site x - c_q is solid (sites
-    outside a non-periodic face count as solid)."""
+    outside a non-periodic face count as solid; across a symmetric z face the
+    upstream site is the mirror image of the boundary layer's)."""
     nx, ny, nz = phase.shape
     I, J, K = np.meshgrid(np.arange(nx), np.arange(ny), np.arange(nz), indexing='ij')
     out = np.zeros((19, nx, ny, nz), bool)
@@ -30,7 +31,9 @@ def solid_source(phase, periodic):
         src = []
         for ax, (c, n, X) in enumerate(zip((CI[q], CJ[q], CK[q]), (nx, ny, nz), (I, J, K))):
             s = X - c
-            if periodic[ax]:
+            if ax == 2 and zsym:
+                s = np.clip(s, 0, n - 1)  # the halo mirrors the adjacent layer
+            elif periodic[ax]:
                 s = s % n
             else:
                 bad |= (s < 0) | (s >= n)
@@ -40,10 +43,21 @@ def solid_source(phase, periodic):
     return torch.from_numpy(out)
 
 
-def stream(f, solid):
+def _zmirror(q):
+    return next(p for p in range(19) if (CI[p], CJ[p], CK[p]) == (CI[q], CJ[q], -CK[q]))
+
+
+def stream(f, solid, zsym=False):
     g = []
     for q in range(19):
         moved = torch.roll(f[q], shifts=(CI[q], CJ[q], CK[q]), dims=(0, 1, 2))
+        if zsym and CK[q] != 0:
+            # pulled across a symmetric z face: the mirrored population of the
+            # mirrored (boundary-layer) site
+            mir = torch.roll(f[_zmirror(q)], shifts=(CI[q], CJ[q], 0), dims=(0, 1, 2))
+            plane = 0 if CK[q] > 0 else -1
+            moved = moved.clone()
+            moved[:, :, plane] = mir[:, :, plane]
         g.append(torch.where(solid[q], f[18 - q], moved))
     return torch.stack(g)
 
@@ -133,9 +147,11 @@ def collide_reg(g, a, we):
     return f, rho, u
 
 
-def run(phase, tau, g, uin, steps, magic=None, scheme='TRT', rho_out=1.0, periodic=(False, False, True)):
-    """Returns the stored velocity of the last step, (3, nx, ny, nz)."""
-    solid = solid_source(phase, periodic)
+def run(phase, tau, g, uin, steps, magic=None, scheme='TRT', rho_out=1.0, periodic=(False, False, True),
+        zsym=False):
+    """Returns the stored velocity of the last step, (3, nx, ny, nz).  zsym:
+    both z faces symmetric."""
+    solid = solid_source(phase, periodic, zsym)
     fluid = torch.from_numpy(phase != 0)
     we = 1.0 / tau
     if scheme == 'TRT':
@@ -146,7 +162,7 @@ def run(phase, tau, g, uin, steps, magic=None, scheme='TRT', rho_out=1.0, period
     f = w[:, None, None, None].expand(19, *phase.shape).clone()
     u = None
     for _ in range(steps):
-        gs = stream(f, solid)
+        gs = stream(f, solid, zsym)
         gs = apply_zou_he(gs, uin, rho_out)
         f, rho, u = collide_reg(gs, g, we) if scheme == 'REG' else collide(gs, g, we, wo)
         f = torch.where(fluid[None], f, w[:, None, None, None].expand_as(f))
