@@ -1005,8 +1005,7 @@ int download(jlb_solver *s, double *den, double *vel) {
 // followed by its FP64 assembly and (on a second stream) its pitched copy to
 // the host while the next slab computes.  The direct step kernel runs this
 // step (the staged kernel's persistent grid does not split into slabs).
-// Used on the copy-engine download path when each slab is whole rows of
-// dense blocks (ny a multiple of the block's rows).
+// Used on the copy-engine download path.
 int final_step_overlapped(jlb_solver *s, double *den, double *vel) {
     const bool pstep = s->parity == 0;
     StepArgs a = make_args(s, 1);
@@ -1035,11 +1034,17 @@ int final_step_overlapped(jlb_solver *s, double *den, double *vel) {
         if ((r = direct(sp, (a.M + 127) / 128))) return r;
     }
     const int kb = a.kblocks;
-    // a thin first slab lets the copies start early; the rest split evenly
+    // a thin first slab lets the copies start early; the rest split evenly.
+    // Slab boundaries fall on whole blocks of rows: plane i starts a block
+    // when i * ny is a multiple of the rows per block
+    int step = rows_per_block;
+    for (int d = rows_per_block; d > 1; --d)
+        if (rows_per_block % d == 0 && s->ny % d == 0) { step = rows_per_block / d; break; }
+    auto snap_i = [&](int i) { return std::min(s->nx, ((i + step - 1) / step) * step); };
     const int first = std::max(1, s->nx / 32);
     auto bound = [&](int k) -> int {
         if (k == 0) return 0;
-        return first + (int)((int64_t)(s->nx - first) * (k - 1) / (nslab - 1));
+        return snap_i(first + (int)((int64_t)(s->nx - first) * (k - 1) / (nslab - 1)));
     };
     for (int k = 0; k < nslab; ++k) {
         const int i0 = bound(k), i1 = k + 1 == nslab ? s->nx : bound(k + 1);
@@ -1047,7 +1052,8 @@ int final_step_overlapped(jlb_solver *s, double *den, double *vel) {
         StepArgs sl = a;
         sl.M = 0;
         sl.b0 = (int)((int64_t)i0 * s->ny / rows_per_block) * kb;
-        sl.nb_dense = (int)((int64_t)(i1 - i0) * s->ny / rows_per_block) * kb;
+        // the last slab may end in a partial block of rows
+        sl.nb_dense = (int)(((int64_t)(i1 - i0) * s->ny + rows_per_block - 1) / rows_per_block) * kb;
         if ((r = direct(sl, sl.nb_dense))) return r;
         // the slab's FP64 assembly follows its step on the compute stream, so
         // that the copy stream carries nothing but back-to-back copies
@@ -1377,7 +1383,7 @@ int jlb_evolve(jlb_solver *s, uint32_t tsteps, const double g[3], double *den, d
     t1 = clk::now();
     if (s->cfg.kernel == JLB_KERNEL_CXX && s->M > 0)
         return fail(s, JLB_ERR_UNSUPPORTED, "the C++-executable kernel has no moving solids");
-    const bool overlap = !overlap_off() && !s->sparse && dma_ready(s, den, vel) && s->ny % make_args(s, 0).by == 0;
+    const bool overlap = !overlap_off() && !s->sparse && dma_ready(s, den, vel);
     r = run_steps(s, overlap ? tsteps - 1 : tsteps, !overlap);
     if (r) return r;
     s->host_t[3] += since(t1);

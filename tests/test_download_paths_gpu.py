@@ -38,7 +38,10 @@ def _run(c, precision, monkeypatch, overlap, dma):
 
 # (nz = 32: 4 rows per block, ny a multiple of 4) and (nz = 128: 1 row per
 # block); nx gives 8 uneven slabs
-CASES = [((16, 8, 32), [0, 0, 0, 3, 0, 0]), ((37, 3, 128), [3, 2, 1, 1, 0, 0]), ((9, 12, 32), [1, 1, 4, 3, 1, 1])]
+CASES = [((16, 8, 32), [0, 0, 0, 3, 0, 0]), ((37, 3, 128), [3, 2, 1, 1, 0, 0]), ((9, 12, 32), [1, 1, 4, 3, 1, 1]),
+         # ny not a multiple of the rows per block (4 at nz = 32, 2 at nz = 64):
+         # slab boundaries on whole blocks, the last slab ends in a partial one
+         ((19, 7, 32), [0, 0, 3, 2, 1, 1]), ((11, 5, 64), [1, 1, 0, 3, 4, 4])]
 
 
 @pytest.mark.parametrize("precision", [0, 1, 2])
@@ -48,6 +51,8 @@ def test_download_paths_agree(ci, precision, monkeypatch):
     c = _case(shape, bc, 1, 40 + ci)
     if bc[3] == 3:
         c["vel0"][:, -1, :, :] = [0.03, 0.0, 0.0]
+    if bc[2] == 3:
+        c["vel0"][:, 0, :, :] = [0.0, 0.02, 0.0]
     f0, out0 = _run(c, precision, monkeypatch, True, True)
     for overlap, dma in ((False, True), (False, False)):
         f1, out1 = _run(c, precision, monkeypatch, overlap, dma)
