@@ -84,7 +84,8 @@ typedef struct jlb_config {
 
 /* Argument validation of Solver.__cinit__ / _check_bc
  * (jyulb/isothermal.pyx:196-206, 378-426).  Writes the reference's message
- * into msg (if not NULL) and returns JLB_ERR_INVALID_ARG on failure. */
+ * into msg (if not NULL) and returns JLB_ERR_INVALID_ARG on failure.  One
+ * check has no reference counterpart: nx * ny must stay below 2^31. */
 int jlb_check_config(const jlb_config *cfg, char *msg, size_t msg_len);
 
 /* Solver.__cinit__ (jyulb/isothermal.pyx:156-298): validate, derive the

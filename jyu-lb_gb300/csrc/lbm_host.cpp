@@ -1088,6 +1088,9 @@ int jlb_check_config(const jlb_config *cfg, char *msg, size_t msg_len) {
     if (!cfg) return bad("Invalid configuration (NULL).");
     if (cfg->lat_size[0] < 1 || cfg->lat_size[1] < 1 || cfg->lat_size[2] < 1)
         return bad("Invalid lattice size input.");
+    // the step kernels index rows of k-lines (i * ny + j) with 32-bit integers
+    if ((int64_t)cfg->lat_size[0] * cfg->lat_size[1] >= ((int64_t)1 << 31))
+        return bad("Lattice too large: nx * ny must stay below 2^31.");
     if (cfg->rlx_scheme != JLB_BGK && cfg->rlx_scheme != JLB_TRT && cfg->rlx_scheme != JLB_REGULARIZATION)
         return bad("Invalid relaxation scheme input.");
     if (!(cfg->kvisc > 0.0)) return bad("Invalid kinematic viscosity input.");

@@ -93,6 +93,10 @@ class Solver:
         if len(lat) < 3 or lat[X] < 1 or lat[Y] < 1 or lat[Z] < 1:
             self.error_msg = 'Invalid lattice size input.'
             raise ValueError(self.error_msg)
+        if lat[X] * lat[Y] >= 2 ** 31:
+            # the step kernels index rows of k-lines with 32-bit integers
+            self.error_msg = 'Lattice too large: nx * ny must stay below 2^31.'
+            raise ValueError(self.error_msg)
         if rlx_scheme not in (BGK, TRT, REGULARIZATION):
             self.error_msg = 'Invalid relaxation scheme input.'
             raise ValueError(self.error_msg)

@@ -59,6 +59,7 @@ def _cfg(**kw):
     (dict(bc=[2, 0, 3, 0, 1, 1]), "Invalid fixed variable bc setup."),
     (dict(bc=[0, 0, 0, 2, 3, 0]), "Invalid fixed variable bc setup."),
     (dict(precision=7), "Invalid precision input."),
+    (dict(lat=[46341, 46341, 1]), "Lattice too large: nx * ny must stay below 2^31."),
 ])
 def test_c_abi_validation_messages(kw, msg):
     lib = _lib()
@@ -80,6 +81,7 @@ def test_c_abi_accepts_valid_configs():
     (((4, 4, 4), 0, -1.0), "Invalid kinematic viscosity input."),
     (((4, 4, 4), 0, 0.1, None, [1, 0, 1, 1, 1, 1]), "Invalid periodic bc setup (in x-dir.)."),
     (((4, 4, 4), 0, 0.1, None, [2, 2, 3, 0, 1, 1]), "Invalid fixed variable bc setup."),
+    (((65536, 32768, 1),), "Lattice too large: nx * ny must stay below 2^31."),
 ])
 def test_solver_validation_raises_value_error(args, msg):
     from jyulb.isothermal import Solver
