@@ -198,8 +198,12 @@ int jlb_reduce_moments_noalloc(const uint32_t *nmask, const void *den, const voi
  * step over a packed node index.  The reference advances one Solver at a
  * time (jyulb/isothermal.pyx:1370-1418); an ensemble of its channels is a
  * loop over Solver objects, which these calls replace.  Populations are
- * FP32 shifted; faces may be WALL or PERIODIC; solids that move must share
- * one velocity per domain (Ladd's term, jyulb/isothermal.pyx:1117-1119).
+ * FP32 shifted.  Domains whose faces are all WALL or PERIODIC and whose
+ * moving solids share one velocity (Ladd's term,
+ * jyulb/isothermal.pyx:1117-1119) run entirely in the packed step kernel;
+ * domains with Zou-He or symmetric faces, or with several solid velocities,
+ * run their boundary nodes through a second launch per step over a
+ * boundary-node list, as the single-domain solver does.
  * --------------------------------------------------------------------- */
 typedef struct jlb_batch jlb_batch;
 
