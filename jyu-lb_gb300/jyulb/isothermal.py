@@ -86,8 +86,12 @@ class Solver:
 
     def __init__(self, lat_size, rlx_scheme=BGK, kvisc=1.0 / 6.0, g=None, bc=None, *,
                  precision=FP64, trt_magic=None, stream=None, kernel='jyulb', stokes=False,
-                 second_order_forcing=False):
+                 second_order_forcing=False, keep_f2=False):
         self.error_msg = ''
+        # the reference's second population buffer is kept only on request
+        # (one population download per evolve call; see the f2 property)
+        self._keep_f2 = bool(keep_f2)
+        self._f2 = None
         lat = [int(v) for v in np.asarray(lat_size).reshape(-1)[:3]]
         # argument checks of jyulb/isothermal.pyx:196-230
         if len(lat) < 3 or lat[X] < 1 or lat[Y] < 1 or lat[Z] < 1:
@@ -237,11 +241,9 @@ class Solver:
     def bc(self):
         return list(self._bc)
 
-    @property
-    def f1(self):
-        """Post-collision populations in the reference's Bundle-C layout
-        (NCNT*19 values, jyulb/isothermal.pyx:1532-1704); halo entries are 0."""
-        f = self.populations()
+    def _bundle_c(self, f):
+        """(19, nx, ny, nz) populations in the reference's Bundle-C layout
+        (NCNT*19 values, jyulb/isothermal.pyx:1532-1704), halo entries 0."""
         NI, NJ, NK, N = self.NI, self.NJ, self.NK, self.NCNT
         full = np.zeros((LVECS, NI, NJ, NK))
         full[:, 1:-1, 1:-1, 1:-1] = f
@@ -251,6 +253,29 @@ class Solver:
         out[5 * N:14 * N].reshape(N, 9)[:] = full[5:14].T
         out[14 * N:].reshape(N, 5)[:] = full[14:19].T
         return out
+
+    @property
+    def f1(self):
+        """Post-collision populations of the latest step in the reference's
+        Bundle-C layout (NCNT*19 values, jyulb/isothermal.pyx:1532-1704);
+        halo entries are 0."""
+        return self._bundle_c(self.populations())
+
+    @property
+    def f2(self):
+        """The reference's second population buffer.  Its evolve swaps f1
+        and f2 after every step (jyulb/isothermal.pyx:1410-1416), so f2 holds
+        the post-collision populations of the step before the latest one
+        (zeros before the first step), in Bundle-C layout; halo entries are 0
+        here.  The in-place AA pattern keeps a single lattice, so a Solver
+        keeps this copy only when built with keep_f2=True: evolve(n) then
+        runs n-1 steps, downloads the populations and runs the last step."""
+        if not self._keep_f2:
+            raise AttributeError('f2 is kept only by a Solver built with keep_f2=True '
+                                 '(the in-place AA pattern has no second lattice)')
+        if self._f2 is None:
+            return np.zeros(LVECS * self.NCNT)
+        return self._bundle_c(self._f2)
 
     # -- update methods --------------------------------------------------------
     def finalize_init(self):
@@ -284,14 +309,35 @@ class Solver:
                                '(i.e. call first the method finalize_init)!')
         if self.fluid_lsite_domain is None:
             return self.tot_tsteps
-        tot = ctypes.c_uint32()
         acc = _native.dptr(self._acc) if self._acc_exposed else None
-        rc = self._lib.jlb_evolve(self._h, int(tsteps), _native.dptr(self._g), _native.dptr(self.den),
+        tsteps = int(tsteps)
+        if not (self._keep_f2 and tsteps > 0):
+            self.tot_tsteps = self._jlb_evolve(tsteps, acc)
+            return self.tot_tsteps
+        if tsteps == 1:
+            prev = self.populations()
+            self.tot_tsteps = self._jlb_evolve(1, acc)
+        else:
+            # n-1 steps, a copy of the populations, then the last step on the
+            # device with the inputs this call read, as inside one evolve(n)
+            self._jlb_evolve(tsteps - 1, acc)
+            prev = self.populations()
+            rc = self._lib.jlb_step(self._h, 1, 1)
+            if rc == _native.JLB_OK:
+                rc = self._lib.jlb_download_moments(self._h, _native.dptr(self.den), _native.dptr(self.vel))
+            if rc != _native.JLB_OK:
+                self._raise(rc)
+            self.tot_tsteps = int(self._lib.jlb_tot_tsteps(self._h))
+        self._f2 = prev
+        return self.tot_tsteps
+
+    def _jlb_evolve(self, tsteps, acc):
+        tot = ctypes.c_uint32()
+        rc = self._lib.jlb_evolve(self._h, tsteps, _native.dptr(self._g), _native.dptr(self.den),
                                   _native.dptr(self.vel), acc, ctypes.byref(tot))
         if rc != _native.JLB_OK:
             self._raise(rc)
-        self.tot_tsteps = int(tot.value)
-        return self.tot_tsteps
+        return int(tot.value)
 
     # -- status ------------------------------------------------------------------
     def error_occured(self):

@@ -41,10 +41,10 @@ def run_oracle(c, chunks=None):
     return nf, o.populations(), o.get_den().copy(), o.get_vel().copy()
 
 
-def make_engine(c, precision=0):
+def make_engine(c, precision=0, **extra):
     from jyulb.isothermal import Solver
 
-    kw = {"precision": precision}
+    kw = {"precision": precision, **extra}
     if c.get("trt_magic"):
         kw["trt_magic"] = c["trt_magic"]
     s = Solver(np.array(c["lat"], dtype=np.int32), c["scheme"], c["kvisc"],
