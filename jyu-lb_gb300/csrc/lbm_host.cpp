@@ -1416,7 +1416,10 @@ int jlb_step(jlb_solver *s, uint32_t tsteps, int write_moments) {
 int jlb_download_moments(jlb_solver *s, double *den, double *vel) {
     if (!s || !den || !vel) return fail(s, JLB_ERR_INVALID_ARG, "NULL argument");
     if (!s->init_done) return fail(s, JLB_ERR_STATE, "finalize_init has not been called");
-    return download(s, den, vel);
+    int r = download(s, den, vel);
+    // steps run by jlb_step are checked here, the first synchronising call
+    if (r == JLB_OK && s->use_tma) r = check_kernel_error(s);
+    return r;
 }
 
 int jlb_get_populations(jlb_solver *s, double *f) {
@@ -1433,7 +1436,8 @@ int jlb_get_populations(jlb_solver *s, double *f) {
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
     cudaFree(tmp);
     CK(e);
-    return JLB_OK;
+    // steps run by jlb_step are checked here, the first synchronising call
+    return s->use_tma ? check_kernel_error(s) : JLB_OK;
 }
 
 int jlb_set_populations(jlb_solver *s, const double *f) {
