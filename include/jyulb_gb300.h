@@ -133,7 +133,9 @@ int jlb_set_acc(jlb_solver *s, const double *acc);
 
 /* Device-only stepping with the inputs of the last jlb_evolve call: no host
  * synchronisation, no host arrays.  write_moments != 0 stores den/vel of the
- * last step on the device (read them with jlb_download_moments). */
+ * last step on the device (read them with jlb_download_moments).  A step
+ * kernel whose bounded wait on its bulk copies ran out is reported by the
+ * next jlb_evolve, jlb_download_moments or jlb_get_populations call. */
 int jlb_step(jlb_solver *s, uint32_t tsteps, int write_moments);
 
 /* copies the device den/vel of the last moment-writing step into the
