@@ -45,6 +45,33 @@ enum Precision { PREC_FP64 = 0, PREC_FP32 = 1, PREC_FP16 = 2 };
 enum Scheme { SCH_BGK = 0, SCH_TRT = 1, SCH_REG = 2 };
 enum Bc { BC_WALL = 0, BC_PERIODIC = 1, BC_FIXED_DEN = 2, BC_FIXED_VEL = 3, BC_SYMMETRIC = 4 };
 
+// Unsigned 32-bit division by a divisor fixed at launch, as a multiply-high
+// and two shifts (Granlund & Montgomery, "Division by invariant integers
+// using multiplication", PLDI 1994, unsigned case with N = 32): for
+// l = ceil(log2 d), m = floor(2^32 (2^l - d) / d) + 1, s1 = min(l, 1),
+// s2 = max(l - 1, 0) and t = mulhi(m, n), n / d = (t + ((n - t) >> s1)) >> s2
+// for every n < 2^32.
+struct UDiv {
+    uint32_t m, s1, s2;
+};
+
+inline UDiv make_udiv(uint32_t d) {
+    uint32_t l = 0;
+    while (l < 32 && ((uint64_t)1 << l) < d) ++l;
+    UDiv u;
+    u.m = (uint32_t)((((uint64_t)1 << 32) * (((uint64_t)1 << l) - d)) / d + 1);
+    u.s1 = l < 1 ? l : 1;
+    u.s2 = l > 1 ? l - 1 : 0;
+    return u;
+}
+
+#ifdef __CUDACC__
+__device__ __forceinline__ uint32_t udiv(uint32_t n, UDiv d) {
+    const uint32_t t = __umulhi(n, d.m);
+    return (t + ((n - t) >> d.s1)) >> d.s2;
+}
+#endif
+
 struct StepArgs {
     void *f;              // populations, 19 * Np elements of the storage type
     int64_t Np;           // slot stride
@@ -60,6 +87,12 @@ struct StepArgs {
     int bx, by, kblocks;  // block shape and k-blocks per row-block
     int nb_dense;         // number of dense blocks; the rest are boundary blocks
     int b0;               // first dense block of this launch (a launch may cover a slab)
+    // linear mapping, used when nz is not a multiple of 32 (a warp along k
+    // alone would leave lanes idle): dense block b takes the sites
+    // [128 b, 128 b + 128) of n = (i*ny + j)*nz + k, with blocks of (128, 1)
+    int lin;
+    uint32_t nsite;       // nx*ny*nz (lin only; below 2^32)
+    UDiv div_nz, div_ny;  // division by nz (lin only) and by ny
     // fluid-only ("sparse") population layout, used on lattices with many
     // solid sites: populations f[q * Npc + m] over the fluid sites m only
     const int32_t *csite; // [Nc] lattice site n of fluid site m

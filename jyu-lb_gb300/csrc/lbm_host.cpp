@@ -20,6 +20,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <numeric>
 #include <string>
 #include <vector>
 
@@ -79,6 +80,7 @@ struct jlb_solver {
     // fluid-only population layout (lattices with many solid sites)
     bool sparse = false;                 // chosen at finalize_init
     bool no_sparse = false;              // the adjoint driver keeps the lattice layout
+    bool no_lin = false;                 // and the row-block mapping of its reverse kernel
     bool c_current = false;              // the fluid-only copy holds the current state
     bool sp_tables_dirty = true;         // boundary tables changed since their translation
     void *fc = nullptr;                  // [19][Npc] populations of the fluid sites
@@ -631,6 +633,15 @@ int upload_dynamic(jlb_solver *s, const double *den, const double *vel) {
     return JLB_OK;
 }
 
+// the linear site mapping of the dense sweep: nz not a multiple of 32, the
+// direct kernel (the staged kernel and the adjoint's reverse kernel tile
+// rows), fewer than 2^32 sites; JLB_LIN=0 keeps the row-block mapping
+bool use_lin(const jlb_solver *s) {
+    const char *e = std::getenv("JLB_LIN");
+    if (e && e[0] == '0') return false;
+    return s->nz % 32 != 0 && !s->use_tma && !s->no_lin && s->N < ((int64_t)1 << 32);
+}
+
 StepArgs make_args(const jlb_solver *s, int write_moments) {
     StepArgs a{};
     a.f = s->f;
@@ -649,6 +660,16 @@ StepArgs make_args(const jlb_solver *s, int write_moments) {
     a.kblocks = (s->nz + a.bx - 1) / a.bx;
     const int64_t rows = (int64_t)s->nx * s->ny;
     a.nb_dense = (int)(a.kblocks * ((rows + a.by - 1) / a.by));
+    a.div_ny = make_udiv((uint32_t)s->ny);
+    if (use_lin(s)) {
+        // nz = 4 would use 4 of 32 lanes, nz = 40 40 of 64: consecutive
+        // sites instead, with (i, j, k) from divisions by nz and ny
+        a.lin = 1;
+        a.bx = 128; a.by = 1; a.kblocks = 1;
+        a.nsite = (uint32_t)s->N;
+        a.div_nz = make_udiv((uint32_t)s->nz);
+        a.nb_dense = (int)((s->N + 127) / 128);
+    }
     a.M = s->M;
     a.sp_node = s->d_sp_node; a.sp_info = s->d_sp_info;
     a.sp_rd = s->d_sp_rd; a.sp_wr = s->d_sp_wr;
@@ -1009,7 +1030,11 @@ int download(jlb_solver *s, double *den, double *vel) {
 int final_step_overlapped(jlb_solver *s, double *den, double *vel) {
     const bool pstep = s->parity == 0;
     StepArgs a = make_args(s, 1);
-    const int rows_per_block = a.by;
+    // a dense block covers block_units of one i-plane's plane_units: rows of
+    // k-lines (times kmul blocks along k), or sites under the linear mapping
+    const int64_t plane_units = a.lin ? (int64_t)s->ny * s->nz : s->ny;
+    const int64_t block_units = a.lin ? 128 : a.by;
+    const int64_t kmul = a.lin ? 1 : a.kblocks;
     auto direct = [&](const StepArgs &x, int blocks) {
         int r;
         if (s->cfg.kernel == JLB_KERNEL_CXX) r = launch_step_cxx(x, s->cfg.rlx_scheme, s->cfg.kernel_opts, pstep, s->accf, blocks, s->st);
@@ -1033,13 +1058,10 @@ int final_step_overlapped(jlb_solver *s, double *den, double *vel) {
         sp.nb_dense = 0;
         if ((r = direct(sp, (a.M + 127) / 128))) return r;
     }
-    const int kb = a.kblocks;
     // a thin first slab lets the copies start early; the rest split evenly.
-    // Slab boundaries fall on whole blocks of rows: plane i starts a block
-    // when i * ny is a multiple of the rows per block
-    int step = rows_per_block;
-    for (int d = rows_per_block; d > 1; --d)
-        if (rows_per_block % d == 0 && s->ny % d == 0) { step = rows_per_block / d; break; }
+    // Slab boundaries fall on whole blocks: plane i starts a block when
+    // i * plane_units is a multiple of block_units
+    const int step = (int)(block_units / std::gcd(block_units, plane_units));
     auto snap_i = [&](int i) { return std::min(s->nx, ((i + step - 1) / step) * step); };
     const int first = std::max(1, s->nx / 32);
     auto bound = [&](int k) -> int {
@@ -1051,9 +1073,9 @@ int final_step_overlapped(jlb_solver *s, double *den, double *vel) {
         if (i1 <= i0) continue;
         StepArgs sl = a;
         sl.M = 0;
-        sl.b0 = (int)((int64_t)i0 * s->ny / rows_per_block) * kb;
-        // the last slab may end in a partial block of rows
-        sl.nb_dense = (int)(((int64_t)(i1 - i0) * s->ny + rows_per_block - 1) / rows_per_block) * kb;
+        sl.b0 = (int)((int64_t)i0 * plane_units / block_units * kmul);
+        // the last slab may end in a partial block
+        sl.nb_dense = (int)(((int64_t)(i1 - i0) * plane_units + block_units - 1) / block_units * kmul);
         if ((r = direct(sl, sl.nb_dense))) return r;
         // the slab's FP64 assembly follows its step on the compute stream, so
         // that the copy stream carries nothing but back-to-back copies
@@ -2198,6 +2220,7 @@ int jlb_adj_create(const jlb_config *cfg, const uint8_t *phase, int32_t loss_pla
     if (r) { std::string m = g_create_error; delete A; return afail(nullptr, r, m); }
     jlb_solver *s = A->s;
     s->no_sparse = true;  // checkpoints and recomputation work on the lattice layout
+    s->no_lin = true;
     // rest state: den = 1, vel = 0 everywhere, so the initial populations do
     // not depend on the parameters
     std::vector<uint8_t> ph((size_t)s->NCNT, 0);

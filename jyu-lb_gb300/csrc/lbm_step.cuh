@@ -162,11 +162,20 @@ template <class ST, class PH, bool PSTEP, bool ACCF, class IT>
 __device__ __forceinline__ void dense_node(const StepArgs &a, int b) {
     using S = typename ST::S;
     using C = typename ST::C;
-    const int kb = b % a.kblocks;
-    const int rb = b / a.kblocks;
-    const int row = rb * a.by + (int)threadIdx.y;
-    const int k = kb * a.bx + (int)threadIdx.x;
-    if (row >= a.nx * a.ny || k >= a.nz) return;
+    int row, k;
+    if (a.lin) {
+        // blocks of (128, 1) over consecutive sites
+        const uint32_t site = (uint32_t)b * 128u + threadIdx.x;
+        if (site >= a.nsite) return;
+        row = (int)udiv(site, a.div_nz);
+        k = (int)(site - (uint32_t)row * (uint32_t)a.nz);
+    } else {
+        const int kb = b % a.kblocks;
+        const int rb = b / a.kblocks;
+        row = rb * a.by + (int)threadIdx.y;
+        k = kb * a.bx + (int)threadIdx.x;
+        if (row >= a.nx * a.ny || k >= a.nz) return;
+    }
     // element indices fit IT (int32 when 19 * Np < 2^31, chosen by the host)
     const IT n = (IT)row * a.nz + k;
     const uint8_t cls = __ldg(a.ncls + n);
@@ -182,7 +191,7 @@ __device__ __forceinline__ void dense_node(const StepArgs &a, int b) {
     // axis; index 0 -> -1, 1 -> 0, 2 -> +1
     IT dI[3], dJ[3], dK[3];
     if (PSTEP) {
-        const int i = row / a.ny;
+        const int i = (int)udiv((uint32_t)row, a.div_ny);
         const int j = row - i * a.ny;
         const IT sI = (IT)a.ny * a.nz, sJ = (IT)a.nz;
         dI[0] = (i == 0 ? (IT)(a.nx - 1) : (IT)-1) * sI;

@@ -41,7 +41,10 @@ def _run(c, precision, monkeypatch, overlap, dma):
 CASES = [((16, 8, 32), [0, 0, 0, 3, 0, 0]), ((37, 3, 128), [3, 2, 1, 1, 0, 0]), ((9, 12, 32), [1, 1, 4, 3, 1, 1]),
          # ny not a multiple of the rows per block (4 at nz = 32, 2 at nz = 64):
          # slab boundaries on whole blocks, the last slab ends in a partial one
-         ((19, 7, 32), [0, 0, 3, 2, 1, 1]), ((11, 5, 64), [1, 1, 0, 3, 4, 4])]
+         ((19, 7, 32), [0, 0, 3, 2, 1, 1]), ((11, 5, 64), [1, 1, 0, 3, 4, 4]),
+         # nz not a multiple of 32: blocks of 128 consecutive sites, slab
+         # boundaries on planes where such a block starts
+         ((21, 6, 5), [0, 0, 0, 3, 0, 0]), ((17, 7, 40), [1, 1, 4, 3, 4, 4])]
 
 
 @pytest.mark.parametrize("precision", [0, 1, 2])
