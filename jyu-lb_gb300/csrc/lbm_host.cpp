@@ -633,13 +633,17 @@ int upload_dynamic(jlb_solver *s, const double *den, const double *vel) {
     return JLB_OK;
 }
 
-// the linear site mapping of the dense sweep: nz not a multiple of 32, the
-// direct kernel (the staged kernel and the adjoint's reverse kernel tile
-// rows), fewer than 2^32 sites; JLB_LIN=0 keeps the row-block mapping
+// the linear site mapping of the dense sweep: wherever the row blocks would
+// leave lanes idle (nz not a multiple of 32, or above 128 and not a multiple
+// of 128), on the direct kernel (the staged kernel and the adjoint's reverse
+// kernel tile rows) and below 2^32 sites; JLB_LIN=0 keeps the row blocks
 bool use_lin(const jlb_solver *s) {
     const char *e = std::getenv("JLB_LIN");
     if (e && e[0] == '0') return false;
-    return s->nz % 32 != 0 && !s->use_tma && !s->no_lin && s->N < ((int64_t)1 << 32);
+    const int nzr = ((s->nz + 31) / 32) * 32;
+    const int bx = nzr >= 128 ? 128 : nzr;
+    const bool idle = (s->nz + bx - 1) / bx * bx != s->nz;
+    return idle && !s->use_tma && !s->no_lin && s->N < ((int64_t)1 << 32);
 }
 
 StepArgs make_args(const jlb_solver *s, int write_moments) {
@@ -719,8 +723,8 @@ int launch_one(jlb_solver *s, const StepArgs &a, bool pstep) {
     return JLB_OK;
 }
 
-// The staged kernel needs 16-byte aligned rows (nz a multiple of 16 bytes of
-// elements), at least one full 128-site tile per row and 32-bit element
+// The staged kernel needs 16-byte aligned rows, whole 128-site tiles per
+// row (nz a multiple of 128) and 32-bit element
 // indices; it only makes sense when most staged sites are fluid.  By default
 // it runs the local (L) step, whose reads are aligned whole rows, and the
 // direct kernel runs the pull-push (P) step: on the 256^3 cavity that split
@@ -745,7 +749,9 @@ void choose_kernel(jlb_solver *s) {
     s->tma_p = e && e[0] == '1';
     if (s->prec == PREC_FP64) return;
     const int pad = (int)(16 / s->ssz);
-    if (s->nz < 128 || s->nz % pad != 0 || s->Np * 19 > 0x7fffffffLL) return;
+    // whole 128-site tiles per row (other nz take the direct kernel with
+    // blocks of consecutive sites)
+    if (s->nz % 128 != 0 || s->nz % pad != 0 || s->Np * 19 > 0x7fffffffLL) return;
     if ((double)s->nfluid < 0.85 * (double)s->N) return;
     const int per_sm = s->prec == PREC_FP32 ? tma_blocks_per_sm_fp32(s->cfg.rlx_scheme)
                                             : tma_blocks_per_sm_fp16(s->cfg.rlx_scheme);

@@ -1,8 +1,9 @@
-"""The dense sweep's two site mappings give identical results.  When nz is
-not a multiple of 32, a block takes 128 consecutive sites (the default);
-JLB_LIN=0 keeps the k-lines of rows that other lattices use.  Lattices with
-Zou-He, symmetric and periodic faces, solids and moving walls, in all three
-storage types; FP64 also against the oracle."""
+"""The dense sweep's two site mappings give identical results.  Where row
+blocks along k would leave lanes idle (nz not a multiple of 32, or above 128
+and not a multiple of 128), a block takes 128 consecutive sites (the
+default); JLB_LIN=0 keeps the k-lines of rows that other lattices use.
+Lattices with Zou-He, symmetric and periodic faces, solids and moving walls,
+in all three storage types; FP64 also against the oracle."""
 import numpy as np
 import pytest
 
@@ -13,7 +14,10 @@ pytestmark = pytest.mark.gpu
 # (shape, bc, solid fraction)
 CASES = [((9, 7, 5), [0, 0, 0, 3, 0, 0], 0.0), ((6, 11, 3), [1, 1, 4, 4, 1, 1], 0.2),
          ((7, 5, 45), [3, 2, 0, 0, 1, 1], 0.1), ((5, 4, 100), [1, 1, 1, 1, 4, 4], 0.15),
-         ((4, 34, 4), [1, 1, 0, 0, 1, 1], 0.0)]
+         ((4, 34, 4), [1, 1, 0, 0, 1, 1], 0.0),
+         # above 128 and not a multiple of 128: row blocks of 128 along k
+         # would leave lanes idle in the second block of each row
+         ((3, 5, 160), [0, 0, 0, 3, 0, 0], 0.0), ((2, 3, 200), [1, 1, 1, 1, 0, 0], 0.1)]
 
 
 def _case(shape, bc, solid, seed):
