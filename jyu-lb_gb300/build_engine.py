@@ -21,6 +21,7 @@ LIB = os.path.join(HERE, "jyulb", "libjyulb_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-std=c++20", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
           "-I", CSRC, "-I", INCLUDE]
+HOST_FLAGS = ["-x", "cu", "-Xcompiler", "-fopenmp", "-Xcompiler", "-ffp-contract=off"]
 UNITS = {
     "lbm_fp64.cu": ["-fmad=false"],
     # resident 128-thread blocks per SM.  The direct steps are latency-bound
@@ -37,11 +38,14 @@ UNITS = {
     "lbm_batch.cu": [],
     "lbm_adjoint.cu": [],
     "lbm_cxx.cu": ["-fmad=false"],
-    # host arithmetic (relaxation rates, Ladd projections) must not be
-    # FMA-contracted either: gcc contracts by default on aarch64
-    "lbm_host.cpp": ["-x", "cu", "-Xcompiler", "-fopenmp", "-Xcompiler", "-ffp-contract=off"],
+    # host arithmetic (relaxation rates, Ladd projections, the adjoint's chain
+    # rule) must not be FMA-contracted either: gcc contracts by default on
+    # aarch64
+    "lbm_host.cpp": HOST_FLAGS,
+    "lbm_batch_host.cpp": HOST_FLAGS,
+    "lbm_adjoint_host.cpp": HOST_FLAGS,
 }
-HEADERS = ["lbm_common.h", "lbm_step.cuh", "lbm_step_tma.cuh", "lbm_shifted.cuh", "lbm_aux.h", "lbm_batch.h", "lbm_adjoint.h"]
+HEADERS = ["lbm_common.h", "lbm_solver.h", "lbm_step.cuh", "lbm_step_tma.cuh", "lbm_shifted.cuh", "lbm_aux.h", "lbm_batch.h", "lbm_adjoint.h"]
 
 
 def _nvcc() -> str:

@@ -11,6 +11,8 @@
 //     reference's Z1 condition, jyulb/isothermal.pyx:500), solid velocities,
 //     previous-step density next to moving solids, acceleration field;
 //   * step sequencing of the AA pair, captured into CUDA graphs.
+// The solver's state (struct jlb_solver) and the helpers the ensemble and
+// adjoint host units reuse are declared in lbm_solver.h.
 #include <cuda_runtime.h>
 #include <omp.h>
 
@@ -27,10 +29,12 @@
 #include "jyulb_gb300.h"
 #include "lbm_aux.h"
 #include "lbm_common.h"
+#include "lbm_solver.h"
 
 using namespace jlb;
+using namespace jlb_host;
 
-namespace {
+namespace jlb_host {
 
 // lattice vectors (reference order)
 const int CI[19] = {-1, -1, -1, -1, -1, 0, 0, 0, 0, 0, 0, 0, 0, 0, 1, 1, 1, 1, 1};
@@ -44,101 +48,6 @@ int find_q(int cx, int cy, int cz) {
 }
 
 thread_local std::string g_create_error;
-
-struct DevBuf {
-    void *p = nullptr;
-    size_t bytes = 0;
-};
-
-} // namespace
-
-struct jlb_solver {
-    jlb_config cfg{};
-    int nx = 0, ny = 0, nz = 0, NI = 0, NJ = 0, NK = 0;
-    int64_t N = 0, Np = 0, NCNT = 0;
-    int prec = 0;
-    size_t ssz = 8, csz = 8;  // storage / compute element sizes
-    double we = 0, wo = 0;
-    double tau = 0;       // relaxation time of the C++-executable model
-    AuxGeom geom{};
-    cudaStream_t st = nullptr;
-    bool own_stream = false;
-
-    // device state
-    void *f = nullptr;
-    uint32_t *nmask = nullptr;
-    uint8_t *ncls = nullptr;
-    void *mom[4] = {nullptr, nullptr, nullptr, nullptr};
-    void *acc = nullptr;
-    double *red_partial = nullptr, *red_out = nullptr;
-    int red_blocks = 0;
-    double *fi_partial = nullptr, *fi_out = nullptr; // flow information (allocated on first use)
-    void *res_prev = nullptr;        // velocity at the last residual call (3 * Np, compute type)
-    double *stg_den = nullptr, *stg_vel = nullptr;   // device copies of the host den/vel layout (DMA download)
-    bool stg_failed = false;
-    cudaStream_t st2 = nullptr;          // download stream of the overlapped last step
-    // fluid-only population layout (lattices with many solid sites)
-    bool sparse = false;                 // chosen at finalize_init
-    bool no_sparse = false;              // the adjoint driver keeps the lattice layout
-    bool no_lin = false;                 // and the row-block mapping of its reverse kernel
-    bool c_current = false;              // the fluid-only copy holds the current state
-    bool sp_tables_dirty = true;         // boundary tables changed since their translation
-    void *fc = nullptr;                  // [19][Npc] populations of the fluid sites
-    int32_t *d_csite = nullptr, *d_cidx = nullptr;
-    int64_t *d_sp_rd_c = nullptr, *d_sp_wr_c = nullptr, *d_sp_cnode = nullptr;
-    int sp_c_cap = 0;
-    int64_t Nc = 0, Npc = 0;
-    std::vector<cudaEvent_t> slab_ev;    // its slab events
-    // boundary-node tables (device)
-    int M = 0, Mcap = 0;
-    int64_t *d_sp_node = nullptr, *d_sp_rd = nullptr, *d_sp_wr = nullptr;
-    uint32_t *d_sp_info = nullptr;
-    double *d_sp_lw = nullptr, *d_sp_bc = nullptr;
-    void *d_sp_den = nullptr;
-
-    // host bookkeeping
-    std::vector<uint8_t> phase;      // halo-padded snapshot after the halo rules
-    std::vector<uint32_t> hmask;     // Np entries
-    std::vector<uint8_t> hcls;       // Np node classes derived from hmask
-    std::vector<int64_t> wall_pos;   // solid positions next to fluid (halo-padded index)
-    std::vector<double> wall_vel;    // their velocities at the last classification
-    std::vector<int64_t> wall_chk;   // indices into wall_pos re-read at every evolve call
-    bool static_halo = false;        // halo cells of closed faces are not written by the caller
-    int64_t *d_wall_pos = nullptr;   // device copies of the checked wall_pos / wall_vel
-    double *d_wall_vel = nullptr;
-    bool wall_dev_dirty = true;      // wall_pos / wall_vel changed since their upload
-    int *wall_flag = nullptr;        // mapped host int set by the check kernel
-    std::vector<int64_t> sp_node;
-    std::vector<uint32_t> sp_info;
-    std::vector<int64_t> sp_rd, sp_wr;
-    std::vector<double> sp_lw;
-    int bc_slots = 0;                // Zou-He data sets per boundary node
-    void *pinned = nullptr;          // staging for per-call uploads
-    size_t pinned_bytes = 0;
-
-    uint64_t nfluid = 0;
-    bool init_done = false;
-    uint32_t tot = 0;
-    int parity = 0;                  // 0: next step is P, 1: next step is L
-    bool accf = false;
-    double g[3] = {0, 0, 0};
-    uint64_t launches = 0;
-    uint64_t h2d_bytes = 0, d2h_bytes = 0; // host<->device traffic issued by the runtime
-    double host_t[6] = {0, 0, 0, 0, 0, 0};  // cumulative seconds per jlb_evolve phase
-    std::string err;
-
-    // graphs of GK consecutive steps without moment output, one per parity
-    cudaGraphExec_t gexec[2] = {nullptr, nullptr};
-    int GK = 32;
-    // bulk-copy staged step (FP32/FP16 on aligned, mostly fluid domains)
-    bool use_tma = false;
-    bool tma_p = true; // also for the pull-push step
-    int tma_grid = 0;
-    int *d_err = nullptr; // set by a kernel whose bounded wait timed out
-    uint64_t args_version = 1, graph_version[2] = {0, 0};
-};
-
-namespace {
 
 int fail(jlb_solver *s, int code, const std::string &msg) {
     if (s) s->err = msg;
@@ -160,10 +69,6 @@ int fail(jlb_solver *s, int code, const std::string &msg) {
         if (r_ != 0) return fail(s, JLB_ERR_CUDA, std::string(#expr) + ": " +                    \
                                  cudaGetErrorString((cudaError_t)r_));                            \
     } while (0)
-
-inline int64_t fidx(const jlb_solver *s, int I, int J, int K) {
-    return ((int64_t)I * s->NJ + J) * s->NK + K;
-}
 
 bool is_fixed(int b) { return b == BC_FIXED_DEN || b == BC_FIXED_VEL; }
 
@@ -1101,7 +1006,7 @@ int final_step_overlapped(jlb_solver *s, double *den, double *vel) {
     return JLB_OK;
 }
 
-} // namespace
+} // namespace jlb_host
 
 // ===========================================================================
 // C ABI
@@ -1573,922 +1478,5 @@ const char *jlb_build_info(void) {
            "FP32 shifted, FP16 storage; BGK/TRT/regularized; bounce-back, Ladd moving walls, Zou-He, "
            "periodic, symmetric";
 }
-
-} // extern "C"
-
-// ===========================================================================
-// Batched ensemble of independent domains (lbm_batch.cu)
-// ===========================================================================
-#include "lbm_batch.h"
-
-struct jlb_batch {
-    int scheme = 0;
-    int ndom = 0;
-    cudaStream_t st = nullptr;
-    bool own_stream = false;
-    std::vector<BatchDomain> dom;
-    std::vector<int32_t> nfluid_dom;
-    int64_t Np = 0, ntot = 0, nfluid = 0;
-    int block = 128, ntiles = 0;
-    // device
-    float *f = nullptr, *dprev = nullptr, *mom[4] = {nullptr, nullptr, nullptr, nullptr};
-    uint8_t *ncls = nullptr;
-    uint32_t *nmask = nullptr, *mmask = nullptr;
-    BatchDomain *d_dom = nullptr;
-    int32_t *tile_dom = nullptr;
-    int parity = 0;
-    uint32_t tot = 0;
-    uint64_t launches = 0;
-    double tune_ms[3] = {0, 0, 0}; // per-step time of blocks 64 / 128 / 256
-    cudaGraphExec_t gexec[2] = {nullptr, nullptr};
-    int GK = 32;
-    // boundary nodes of domains with Zou-He or symmetric faces (device
-    // tables in the single-domain layout, element indices into f)
-    int Msp = 0;
-    std::vector<int> sp_first;    // [ndom + 1]: domain d owns boundary nodes [sp_first[d], sp_first[d+1])
-    int32_t *d_sp_dom = nullptr;
-    int64_t *d_sp_node = nullptr, *d_sp_rd = nullptr, *d_sp_wr = nullptr;
-    uint32_t *d_sp_info = nullptr;
-    double *d_sp_lw = nullptr, *d_sp_bc = nullptr;
-    float *d_sp_den = nullptr;
-    std::string err;
-};
-
-namespace {
-
-int bfail(jlb_batch *b, int code, const std::string &m) {
-    if (b) b->err = m;
-    else g_create_error = m;
-    return code;
-}
-
-#define BCK(call)                                                                                  \
-    do {                                                                                           \
-        cudaError_t e_ = (call);                                                                   \
-        if (e_ != cudaSuccess)                                                                     \
-            return bfail(b, e_ == cudaErrorMemoryAllocation ? JLB_ERR_NOMEM : JLB_ERR_CUDA,        \
-                         std::string(#call) + ": " + cudaGetErrorString(e_));                      \
-    } while (0)
-
-BatchArgs batch_args(const jlb_batch *b, int write_moments) {
-    BatchArgs a{};
-    a.f = b->f;
-    a.Np = b->Np;
-    for (int q = 0; q < 19; ++q) a.fq[q] = b->f + (size_t)q * b->Np;
-    a.dom = b->d_dom;
-    a.tile_dom = b->tile_dom;
-    a.ncls = b->ncls;
-    a.nmask = b->nmask;
-    a.mmask = b->mmask;
-    a.dprev = b->dprev;
-    a.den = b->mom[0]; a.ux = b->mom[1]; a.uy = b->mom[2]; a.uz = b->mom[3];
-    a.write_moments = write_moments;
-    a.Msp = b->Msp;
-    a.sp_dom = b->d_sp_dom;
-    a.sp_node = b->d_sp_node; a.sp_rd = b->d_sp_rd; a.sp_wr = b->d_sp_wr;
-    a.sp_info = b->d_sp_info;
-    a.sp_lw = b->d_sp_lw; a.sp_bc = b->d_sp_bc;
-    a.sp_den = b->d_sp_den;
-    return a;
-}
-
-// tile table for block size `block`; also sets first_tile of every domain
-int batch_tiles(jlb_batch *b, int block) {
-    std::vector<int32_t> td;
-    for (int d = 0; d < b->ndom; ++d) {
-        b->dom[d].first_tile = (int32_t)td.size();
-        const int nt = (b->dom[d].n + block - 1) / block;
-        for (int t = 0; t < nt; ++t) td.push_back(d);
-    }
-    b->ntiles = (int)td.size();
-    b->block = block;
-    if (b->tile_dom) cudaFree(b->tile_dom);
-    b->tile_dom = nullptr;
-    BCK(cudaMalloc(&b->tile_dom, td.size() * sizeof(int32_t)));
-    BCK(cudaMemcpyAsync(b->tile_dom, td.data(), td.size() * sizeof(int32_t), cudaMemcpyHostToDevice, b->st));
-    BCK(cudaMemcpyAsync(b->d_dom, b->dom.data(), b->dom.size() * sizeof(BatchDomain), cudaMemcpyHostToDevice,
-                        b->st));
-    BCK(cudaStreamSynchronize(b->st));
-    for (int p = 0; p < 2; ++p) {
-        if (b->gexec[p]) cudaGraphExecDestroy(b->gexec[p]);
-        b->gexec[p] = nullptr;
-    }
-    return JLB_OK;
-}
-
-int batch_launch(jlb_batch *b, bool pstep, int write_moments) {
-    const BatchArgs a = batch_args(b, write_moments);
-    int r = launch_batch_step(a, b->scheme, pstep, b->block, b->ntiles, b->st);
-    if (r) return bfail(b, JLB_ERR_CUDA, std::string("batch step: ") + cudaGetErrorString((cudaError_t)r));
-    ++b->launches;
-    if (b->Msp > 0) {
-        r = launch_batch_special(a, b->scheme, pstep, b->st);
-        if (r) return bfail(b, JLB_ERR_CUDA, std::string("batch boundary nodes: ") + cudaGetErrorString((cudaError_t)r));
-        ++b->launches;
-    }
-    return JLB_OK;
-}
-
-int batch_run(jlb_batch *b, uint32_t n, bool write_last) {
-    uint32_t plain = write_last && n > 0 ? n - 1 : n;
-    while (graphs_enabled() && plain >= (uint32_t)b->GK) {
-        const int p = b->parity;
-        if (!b->gexec[p]) {
-            cudaGraph_t g;
-            BCK(cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal));
-            int par = p, rr = JLB_OK;
-            for (int t = 0; t < b->GK && rr == JLB_OK; ++t) {
-                rr = batch_launch(b, par == 0, 0);
-                par ^= 1;
-            }
-            cudaError_t ce = cudaStreamEndCapture(b->st, &g);
-            if (rr) return rr;
-            if (ce != cudaSuccess) return bfail(b, JLB_ERR_CUDA, "batch graph capture failed");
-            b->launches -= (uint64_t)b->GK * (1 + (b->Msp > 0));
-            ce = cudaGraphInstantiate(&b->gexec[p], g, 0);
-            cudaGraphDestroy(g);
-            if (ce != cudaSuccess) return bfail(b, JLB_ERR_CUDA, "batch graph instantiate failed");
-        }
-        BCK(cudaGraphLaunch(b->gexec[p], b->st));
-        b->launches += (uint64_t)b->GK * (1 + (b->Msp > 0));
-        plain -= b->GK;
-        if (b->GK & 1) b->parity ^= 1;
-    }
-    for (uint32_t t = 0; t < plain; ++t) {
-        int r = batch_launch(b, b->parity == 0, 0);
-        if (r) return r;
-        b->parity ^= 1;
-    }
-    if (write_last && n > 0) {
-        int r = batch_launch(b, b->parity == 0, 1);
-        if (r) return r;
-        b->parity ^= 1;
-    }
-    return JLB_OK;
-}
-
-// times 2 warm-up + 4 steps for each block size on the current state, then
-// restores the state; keeps the fastest block size
-int batch_autotune(jlb_batch *b) {
-    const size_t fb = (size_t)19 * b->Np * sizeof(float), db = (size_t)b->Np * sizeof(float);
-    float *fsave = nullptr, *dsave = nullptr;
-    if (cudaMalloc(&fsave, fb) != cudaSuccess || cudaMalloc(&dsave, db) != cudaSuccess) {
-        cudaGetLastError();
-        if (fsave) cudaFree(fsave);
-        return batch_tiles(b, 128); // no room for a scratch copy: keep the default
-    }
-    BCK(cudaMemcpyAsync(fsave, b->f, fb, cudaMemcpyDeviceToDevice, b->st));
-    BCK(cudaMemcpyAsync(dsave, b->dprev, db, cudaMemcpyDeviceToDevice, b->st));
-    std::vector<float> spsave((size_t)b->Msp);
-    if (b->Msp > 0)
-        BCK(cudaMemcpyAsync(spsave.data(), b->d_sp_den, spsave.size() * sizeof(float), cudaMemcpyDeviceToHost, b->st));
-    const int cand[3] = {64, 128, 256};
-    int best = 128;
-    double best_ms = 1e30;
-    cudaEvent_t e0, e1;
-    cudaEventCreate(&e0);
-    cudaEventCreate(&e1);
-    for (int c = 0; c < 3; ++c) {
-        int r = batch_tiles(b, cand[c]);
-        if (r) return r;
-        for (int t = 0; t < 2; ++t) if ((r = batch_launch(b, t == 0, 0))) return r;
-        cudaEventRecord(e0, b->st);
-        for (int t = 0; t < 4; ++t) if ((r = batch_launch(b, t % 2 == 0, 0))) return r;
-        cudaEventRecord(e1, b->st);
-        cudaEventSynchronize(e1);
-        float ms = 0;
-        cudaEventElapsedTime(&ms, e0, e1);
-        b->tune_ms[c] = ms / 4.0;
-        if (ms < best_ms) { best_ms = ms; best = cand[c]; }
-    }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    b->launches -= 18 * (1 + (b->Msp > 0)); // tuning steps are not part of the run
-    BCK(cudaMemcpyAsync(b->f, fsave, fb, cudaMemcpyDeviceToDevice, b->st));
-    BCK(cudaMemcpyAsync(b->dprev, dsave, db, cudaMemcpyDeviceToDevice, b->st));
-    if (b->Msp > 0)
-        BCK(cudaMemcpyAsync(b->d_sp_den, spsave.data(), spsave.size() * sizeof(float), cudaMemcpyHostToDevice, b->st));
-    BCK(cudaStreamSynchronize(b->st));
-    cudaFree(fsave);
-    cudaFree(dsave);
-    return batch_tiles(b, best);
-}
-
-} // namespace
-
-extern "C" {
-
-void jlb_batch_destroy(jlb_batch *b) {
-    if (!b) return;
-    if (b->st) cudaStreamSynchronize(b->st);
-    for (int p = 0; p < 2; ++p)
-        if (b->gexec[p]) cudaGraphExecDestroy(b->gexec[p]);
-    void *bufs[] = {b->f, b->dprev, b->mom[0], b->mom[1], b->mom[2], b->mom[3], b->ncls, b->nmask, b->mmask,
-                    b->d_dom, b->tile_dom, b->d_sp_dom, b->d_sp_node, b->d_sp_rd, b->d_sp_wr, b->d_sp_info,
-                    b->d_sp_lw, b->d_sp_bc, b->d_sp_den};
-    for (void *p : bufs)
-        if (p) cudaFree(p);
-    if (b->own_stream && b->st) cudaStreamDestroy(b->st);
-    delete b;
-}
-
-int jlb_batch_create(int32_t scheme, const jlb_domain *doms, int32_t ndom, void *stream, jlb_batch **out) {
-    jlb_batch *b = nullptr;
-    if (!out || !doms || ndom < 1) return bfail(nullptr, JLB_ERR_INVALID_ARG, "no domains");
-    *out = nullptr;
-    if (scheme < JLB_BGK || scheme > JLB_REGULARIZATION) return bfail(nullptr, JLB_ERR_INVALID_ARG, "Invalid relaxation scheme input.");
-    b = new jlb_batch();
-    b->scheme = scheme;
-    b->ndom = ndom;
-    auto bail = [&](int code) {
-        std::string m = b->err;
-        jlb_batch_destroy(b);
-        bfail(nullptr, code, m);
-        return code;
-    };
-    if (stream) b->st = (cudaStream_t)stream;
-    else {
-        if (cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking) != cudaSuccess) {
-            b->err = "cudaStreamCreate failed";
-            return bail(JLB_ERR_CUDA);
-        }
-        b->own_stream = true;
-    }
-    // layout
-    int64_t off = 0;
-    b->dom.resize(ndom);
-    for (int d = 0; d < ndom; ++d) {
-        const jlb_domain &D = doms[d];
-        jlb_config cfg{};
-        for (int a = 0; a < 3; ++a) cfg.lat_size[a] = D.lat_size[a];
-        cfg.rlx_scheme = scheme;
-        cfg.kvisc = D.kvisc;
-        for (int a = 0; a < 3; ++a) cfg.g[a] = D.g[a];
-        for (int f = 0; f < 6; ++f) cfg.bc[f] = D.bc[f];
-        cfg.precision = JLB_FP32;
-        cfg.trt_magic = D.trt_magic;
-        char msg[256];
-        if (jlb_check_config(&cfg, msg, sizeof msg) != JLB_OK) {
-            b->err = "domain " + std::to_string(d) + ": " + msg;
-            return bail(JLB_ERR_INVALID_ARG);
-        }
-
-        if (!D.phase) { b->err = "domain " + std::to_string(d) + ": phase is NULL"; return bail(JLB_ERR_INVALID_ARG); }
-        BatchDomain &B = b->dom[d];
-        B.nx = D.lat_size[0]; B.ny = D.lat_size[1]; B.nz = D.lat_size[2];
-        const int64_t n = (int64_t)B.nx * B.ny * B.nz;
-        if (off + n >= 0x7fffff00LL) { b->err = "ensemble exceeds 2^31 sites"; return bail(JLB_ERR_UNSUPPORTED); }
-        B.off = (int32_t)off;
-        B.n = (int32_t)n;
-        B.inv_syz = 1.0f / (float)(B.ny * B.nz);
-        B.inv_nz = 1.0f / (float)B.nz;
-        for (int f = 0; f < 6; ++f) B.bc[f] = D.bc[f];
-        off += ((n + 127) / 128) * 128;
-        const double tau_e = 0.5 + 3.0 * D.kvisc;
-        const double we = 1.0 / tau_e;
-        double wo = we;
-        if (scheme == JLB_TRT)
-            wo = D.trt_magic > 0.0 ? 1.0 / (D.trt_magic / (tau_e - 0.5) + 0.5) : 8.0 * (2.0 - we) / (8.0 - we);
-        B.we = (float)we; B.wo = (float)wo;
-        for (int a = 0; a < 3; ++a) { B.g[a] = (float)D.g[a]; B.uw[a] = 0.0f; }
-    }
-    b->ntot = off;
-    b->Np = off;
-    auto alloc = [&](void **p, size_t bytes) {
-        if (cudaMalloc(p, bytes) != cudaSuccess) {
-            cudaGetLastError();
-            b->err = "device allocation of " + std::to_string(bytes) + " bytes failed";
-            return JLB_ERR_NOMEM;
-        }
-        return JLB_OK;
-    };
-    int r;
-    if ((r = alloc((void **)&b->f, (size_t)19 * b->Np * sizeof(float)))) return bail(r);
-    if ((r = alloc((void **)&b->dprev, (size_t)b->Np * sizeof(float)))) return bail(r);
-    for (int c = 0; c < 4; ++c)
-        if ((r = alloc((void **)&b->mom[c], (size_t)b->Np * sizeof(float)))) return bail(r);
-    if ((r = alloc((void **)&b->ncls, (size_t)b->Np))) return bail(r);
-    if ((r = alloc((void **)&b->nmask, (size_t)b->Np * sizeof(uint32_t)))) return bail(r);
-    if ((r = alloc((void **)&b->mmask, (size_t)b->Np * sizeof(uint32_t)))) return bail(r);
-    if ((r = alloc((void **)&b->d_dom, (size_t)ndom * sizeof(BatchDomain)))) return bail(r);
-    cudaMemsetAsync(b->ncls, BCLS_SOLID, (size_t)b->Np, b->st);
-    cudaMemsetAsync(b->dprev, 0, (size_t)b->Np * sizeof(float), b->st);
-    // per domain: halo rules, masks and initial populations of a single-domain
-    // FP32 solver, packed into the ensemble arrays
-    std::vector<uint8_t> cls;
-    std::vector<uint32_t> mm, lm;
-    std::vector<float> dp;
-    b->nfluid_dom.assign(ndom, 0);
-    // boundary nodes of domains with Zou-He or symmetric faces, per node:
-    // domain, packed node, info, 19 read / write elements, 19 c.u_wall, 2 x 4
-    // Zou-He values, previous density
-    std::vector<int32_t> g_dom;
-    std::vector<int64_t> g_node;
-    std::vector<uint32_t> g_info;
-    std::vector<int64_t> g_rd, g_wr;   // node-major [t][19] until the upload
-    std::vector<double> g_lw, g_bc;    // [t][19], [t][8]
-    std::vector<float> g_den;
-    b->sp_first.assign(ndom + 1, 0);
-    for (int d = 0; d < ndom; ++d) {
-        const jlb_domain &D = doms[d];
-        BatchDomain &B = b->dom[d];
-        jlb_config cfg{};
-        for (int a = 0; a < 3; ++a) cfg.lat_size[a] = D.lat_size[a];
-        cfg.rlx_scheme = scheme;
-        cfg.kvisc = D.kvisc;
-        for (int a = 0; a < 3; ++a) cfg.g[a] = D.g[a];
-        for (int f = 0; f < 6; ++f) cfg.bc[f] = D.bc[f];
-        cfg.precision = JLB_FP32;
-        cfg.trt_magic = D.trt_magic;
-        cfg.stream = b->st;
-        jlb_solver *s = nullptr;
-        if ((r = jlb_create(&cfg, &s))) { b->err = "domain " + std::to_string(d) + ": " + g_create_error; return bail(r); }
-        const int NI = B.nx + 2, NJ = B.ny + 2, NK = B.nz + 2;
-        const size_t ncnt = (size_t)NI * NJ * NK;
-        std::vector<uint8_t> ph(ncnt, 0);
-        std::vector<double> den(ncnt, 1.0), vel(3 * ncnt, 0.0);
-        for (int i = 0; i < B.nx; ++i)
-            for (int j = 0; j < B.ny; ++j)
-                for (int k = 0; k < B.nz; ++k) {
-                    const size_t li = ((size_t)i * B.ny + j) * B.nz + k;
-                    const size_t fi = ((size_t)(i + 1) * NJ + (j + 1)) * NK + (k + 1);
-                    ph[fi] = D.phase[li];
-                    if (D.den) den[fi] = D.den[li];
-                    if (D.vel) for (int a = 0; a < 3; ++a) vel[3 * fi + a] = D.vel[3 * li + a];
-                }
-        uint64_t nf = 0;
-        r = jlb_finalize_init(s, ph.data(), den.data(), vel.data(), &nf);
-        if (r) { b->err = "domain " + std::to_string(d) + ": " + s->err; jlb_destroy(s); return bail(r); }
-        b->nfluid_dom[d] = (int32_t)nf;
-        b->nfluid += (int64_t)nf;
-        if (nf > 0) {
-            r = launch_batch_pack((const float *)s->f, s->Np, B.n, b->f, b->Np, B.off, b->st);
-            if (r) { b->err = "pack kernel failed"; jlb_destroy(s); return bail(JLB_ERR_CUDA); }
-        }
-        // boundary nodes of a domain with Zou-He or symmetric faces take the
-        // table path (with their moving-wall links); the tables translate the
-        // single-domain element indices q * Np_d + m into the packed array
-        bool routed = false;
-        for (int f = 0; f < 6; ++f)
-            routed |= D.bc[f] == JLB_FIXED_DEN || D.bc[f] == JLB_FIXED_VEL || D.bc[f] == JLB_SYMMETRIC;
-        // so do domains whose moving solids have more than one velocity (the
-        // packed kernel's Ladd term takes one velocity per domain)
-        if (!routed && D.vel) {
-            const double *v0 = nullptr;
-            for (int64_t l = 0; l < B.n && !routed; ++l) {
-                if (D.phase[l] != 0) continue;
-                const double *u = D.vel + 3 * l;
-                if (u[0] == 0.0 && u[1] == 0.0 && u[2] == 0.0) continue;
-                if (!v0) v0 = u;
-                else routed = u[0] != v0[0] || u[1] != v0[1] || u[2] != v0[2];
-            }
-        }
-        b->sp_first[d] = (int)g_node.size();
-        if (routed && nf > 0 && s->M > 0) {
-            const int M = s->M;
-            std::vector<double> bcbuf((size_t)8 * M, 0.0);
-            std::vector<float> denbuf((size_t)M, 0.0f);
-            fill_dynamic(s, den.data(), vel.data(), bcbuf.data(), denbuf.data());
-            const int64_t Npd = s->Np;
-            auto tr = [&](int64_t e) { return (e / Npd) * b->Np + B.off + (e % Npd); };
-            for (int t = 0; t < M; ++t) {
-                g_dom.push_back(d);
-                g_node.push_back(B.off + s->sp_node[t]);
-                g_info.push_back(s->sp_info[t]);
-                for (int q = 0; q < 19; ++q) {
-                    g_rd.push_back(tr(s->sp_rd[(size_t)q * M + t]));
-                    g_wr.push_back(tr(s->sp_wr[(size_t)q * M + t]));
-                    g_lw.push_back(s->sp_lw[(size_t)q * M + t]);
-                }
-                for (int c = 0; c < 8; ++c) g_bc.push_back(c < 4 * s->bc_slots ? bcbuf[(size_t)c * M + t] : 0.0);
-                g_den.push_back(denbuf[t]);
-            }
-        }
-        b->sp_first[d + 1] = (int)g_node.size();
-        // node classes and masks; the moving solids of a domain share one velocity
-        cls.assign(B.n, BCLS_SOLID);
-        lm.assign(B.n, 0);
-        mm.assign(B.n, 0);
-        dp.assign(B.n, 0.0f);
-        bool have_uw = false;
-        double uw[3] = {0, 0, 0};
-        for (int64_t l = 0; l < B.n && nf > 0; ++l) {
-            const uint32_t m = s->hmask[l];
-            if (m & MASK_SOLID) continue;
-            const int i = (int)(l / ((int64_t)B.ny * B.nz)), j = (int)((l / B.nz) % B.ny), k = (int)(l % B.nz);
-            if (routed && (m & MASK_SPECIAL)) {
-                lm[l] = m & MASK_LINKS;
-                cls[l] = BCLS_SPECIAL;
-                continue;
-            }
-            uint32_t mv = 0;
-            for (int q = 0; q < 19; ++q) {
-                if (!(m & (1u << q))) continue;
-                const size_t sp = ((size_t)(i + 1 - CI[q]) * NJ + (j + 1 - CJ[q])) * NK + (k + 1 - CK[q]);
-                const double *u = vel.data() + 3 * sp;
-                if (u[0] == 0.0 && u[1] == 0.0 && u[2] == 0.0) continue;
-                if (!have_uw) { uw[0] = u[0]; uw[1] = u[1]; uw[2] = u[2]; have_uw = true; }
-                else if (u[0] != uw[0] || u[1] != uw[1] || u[2] != uw[2]) {
-                    b->err = "domain " + std::to_string(d) + ": moving solids of one batched domain must share one velocity";
-                    jlb_destroy(s);
-                    return bail(JLB_ERR_UNSUPPORTED);
-                }
-                mv |= 1u << q;
-            }
-            lm[l] = m & MASK_LINKS;
-            mm[l] = mv;
-            cls[l] = mv ? BCLS_MOVING : (m & MASK_LINKS) ? BCLS_WALL : BCLS_PLAIN;
-            const size_t fi = ((size_t)(i + 1) * NJ + (j + 1)) * NK + (k + 1);
-            dp[l] = (float)(den[fi] - 1.0);
-        }
-        for (int a = 0; a < 3; ++a) B.uw[a] = (float)uw[a];
-        cudaError_t e1 = cudaMemcpyAsync(b->ncls + B.off, cls.data(), B.n, cudaMemcpyHostToDevice, b->st);
-        cudaError_t e2 = cudaMemcpyAsync(b->nmask + B.off, lm.data(), (size_t)B.n * 4, cudaMemcpyHostToDevice, b->st);
-        cudaError_t e3 = cudaMemcpyAsync(b->mmask + B.off, mm.data(), (size_t)B.n * 4, cudaMemcpyHostToDevice, b->st);
-        cudaError_t e4 = cudaMemcpyAsync(b->dprev + B.off, dp.data(), (size_t)B.n * 4, cudaMemcpyHostToDevice, b->st);
-        cudaError_t e5 = cudaStreamSynchronize(b->st); // host vectors are reused next domain
-        jlb_destroy(s);
-        if (e1 || e2 || e3 || e4 || e5) { b->err = "domain upload failed"; return bail(JLB_ERR_CUDA); }
-    }
-    b->Msp = (int)g_node.size();
-    if (b->Msp > 0) {
-        const int M = b->Msp;
-        // node-major [t][19] -> [19][M] as the boundary-node path reads them
-        std::vector<int64_t> rd((size_t)19 * M), wr((size_t)19 * M);
-        std::vector<double> lw((size_t)19 * M), bcd((size_t)8 * M);
-        for (int t = 0; t < M; ++t) {
-            for (int q = 0; q < 19; ++q) {
-                rd[(size_t)q * M + t] = g_rd[(size_t)t * 19 + q];
-                wr[(size_t)q * M + t] = g_wr[(size_t)t * 19 + q];
-                lw[(size_t)q * M + t] = g_lw[(size_t)t * 19 + q];
-            }
-            for (int c = 0; c < 8; ++c) bcd[(size_t)c * M + t] = g_bc[(size_t)t * 8 + c];
-        }
-        if ((r = alloc((void **)&b->d_sp_dom, (size_t)M * 4)) || (r = alloc((void **)&b->d_sp_node, (size_t)M * 8)) ||
-            (r = alloc((void **)&b->d_sp_info, (size_t)M * 4)) || (r = alloc((void **)&b->d_sp_rd, rd.size() * 8)) ||
-            (r = alloc((void **)&b->d_sp_wr, wr.size() * 8)) || (r = alloc((void **)&b->d_sp_lw, lw.size() * 8)) ||
-            (r = alloc((void **)&b->d_sp_bc, bcd.size() * 8)) || (r = alloc((void **)&b->d_sp_den, (size_t)M * 4)))
-            return bail(r);
-        cudaError_t e = cudaSuccess;
-        auto up = [&](void *dst, const void *src, size_t n) {
-            if (e == cudaSuccess) e = cudaMemcpy(dst, src, n, cudaMemcpyHostToDevice);
-        };
-        up(b->d_sp_dom, g_dom.data(), (size_t)M * 4);
-        up(b->d_sp_node, g_node.data(), (size_t)M * 8);
-        up(b->d_sp_info, g_info.data(), (size_t)M * 4);
-        up(b->d_sp_rd, rd.data(), rd.size() * 8);
-        up(b->d_sp_wr, wr.data(), wr.size() * 8);
-        up(b->d_sp_lw, lw.data(), lw.size() * 8);
-        up(b->d_sp_bc, bcd.data(), bcd.size() * 8);
-        up(b->d_sp_den, g_den.data(), (size_t)M * 4);
-        if (e != cudaSuccess) { b->err = "boundary-node table upload failed"; return bail(JLB_ERR_CUDA); }
-    }
-    const char *tune = std::getenv("JLB_BATCH_BLOCK");
-    if (tune && tune[0]) r = batch_tiles(b, std::atoi(tune));
-    else r = batch_autotune(b);
-    if (r) return bail(r);
-    *out = b;
-    return JLB_OK;
-}
-
-int jlb_batch_step(jlb_batch *b, uint32_t tsteps) {
-    if (!b) return bfail(b, JLB_ERR_INVALID_ARG, "NULL batch");
-    int r = batch_run(b, tsteps, true);
-    if (r) return r;
-    b->tot += tsteps;
-    return JLB_OK;
-}
-
-int jlb_batch_moments(jlb_batch *b, int32_t d, double *den, double *vel) {
-    if (!b || d < 0 || d >= b->ndom || !den || !vel) return bfail(b, JLB_ERR_INVALID_ARG, "bad argument");
-    const BatchDomain &B = b->dom[d];
-    std::vector<float> h((size_t)4 * B.n);
-    for (int c = 0; c < 4; ++c)
-        BCK(cudaMemcpyAsync(h.data() + (size_t)c * B.n, b->mom[c] + B.off, (size_t)B.n * 4, cudaMemcpyDeviceToHost,
-                            b->st));
-    std::vector<uint8_t> cl(B.n);
-    BCK(cudaMemcpyAsync(cl.data(), b->ncls + B.off, B.n, cudaMemcpyDeviceToHost, b->st));
-    BCK(cudaStreamSynchronize(b->st));
-    for (int32_t l = 0; l < B.n; ++l) {
-        if (cl[l] == BCLS_SOLID) continue; // solid sites keep the caller's values
-        den[l] = 1.0 + (double)h[l];
-        for (int a = 0; a < 3; ++a) vel[3 * (size_t)l + a] = (double)h[(size_t)(a + 1) * B.n + l];
-    }
-    return JLB_OK;
-}
-
-int jlb_batch_populations(jlb_batch *b, int32_t d, double *f) {
-    if (!b || d < 0 || d >= b->ndom || !f) return bfail(b, JLB_ERR_INVALID_ARG, "bad argument");
-    const BatchDomain &B = b->dom[d];
-    double *tmp = nullptr;
-    BCK(cudaMalloc(&tmp, (size_t)19 * B.n * sizeof(double)));
-    int r = launch_batch_readout(batch_args(b, 0), d, B.n, b->parity, b->sp_first[d], b->sp_first[d + 1], tmp,
-                                 b->st);
-    cudaError_t e = r ? (cudaError_t)r
-                      : cudaMemcpyAsync(f, tmp, (size_t)19 * B.n * sizeof(double), cudaMemcpyDeviceToHost, b->st);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(b->st);
-    cudaFree(tmp);
-    BCK(e);
-    return JLB_OK;
-}
-
-int jlb_batch_info(const jlb_batch *b, int64_t out[8]) {
-    if (!b || !out) return JLB_ERR_INVALID_ARG;
-    out[0] = b->ntot;
-    out[1] = b->nfluid;
-    out[2] = b->block;
-    out[3] = b->ntiles;
-    out[4] = (int64_t)b->launches;
-    out[5] = (int64_t)(b->tune_ms[0] * 1e3);
-    out[6] = (int64_t)(b->tune_ms[1] * 1e3);
-    out[7] = (int64_t)(b->tune_ms[2] * 1e3);
-    return JLB_OK;
-}
-
-int32_t jlb_batch_domain_fluid(const jlb_batch *b, int32_t d) {
-    return (b && d >= 0 && d < b->ndom) ? b->nfluid_dom[d] : -1;
-}
-
-const char *jlb_batch_last_error(const jlb_batch *b) { return b ? b->err.c_str() : g_create_error.c_str(); }
-
-} // extern "C"
-
-// ===========================================================================
-// Adjoint of the time step with checkpointing (lbm_adjoint.cu)
-// ===========================================================================
-#include "lbm_adjoint.h"
-
-struct jlb_adjoint {
-    jlb_solver *s = nullptr;
-    int K = 50;               // checkpoint interval
-    int plane = 0;
-    double magic = 0.0;       // TRT magic parameter (<= 0: reference's 3/16)
-    void *f0 = nullptr;       // initial populations
-    std::vector<void *> ckpt; // populations before steps 0, K, 2K, ...
-    // recompute buffers, nsets sets of K: set p holds the states before the
-    // steps of a segment in snap[p*K + 1 .. p*K + K-1] (snap[p*K] is scratch)
-    // and their boundary-site collision inputs in sp_in[p][K][19][M]; with two
-    // sets the recompute of one segment overlaps the reverse sweep of the next
-    std::vector<void *> snap;
-    void *sp_in = nullptr;
-    int nsets = 0;
-    cudaStream_t st2 = nullptr; // recompute stream
-    void *lam = nullptr;
-    double *d_target = nullptr, *d_part = nullptr, *d_guin = nullptr;
-    int nparts = 0;           // per-block sensitivity slots
-    uint32_t steps = 0;
-    double tau = 1.0;
-    bool have_forward = false;
-    size_t fbytes = 0;
-    std::vector<cudaEvent_t> ev; // forward pair, backward pair, then 4 per backward segment
-    double ms[4] = {0, 0, 0, 0};  // forward, recompute, reverse sweep, whole backward
-    std::string err;
-};
-
-namespace {
-
-int afail(jlb_adjoint *A, int code, const std::string &m) {
-    if (A) A->err = m;
-    else g_create_error = m;
-    return code;
-}
-
-#define ACK(call)                                                                                  \
-    do {                                                                                           \
-        cudaError_t e_ = (call);                                                                   \
-        if (e_ != cudaSuccess)                                                                     \
-            return afail(A, e_ == cudaErrorMemoryAllocation ? JLB_ERR_NOMEM : JLB_ERR_CUDA,        \
-                         std::string(#call) + ": " + cudaGetErrorString(e_));                      \
-    } while (0)
-
-// the first n timing events, created on first use
-cudaError_t adj_events(jlb_adjoint *A, size_t n) {
-    while (A->ev.size() < n) {
-        cudaEvent_t e;
-        const cudaError_t r = cudaEventCreate(&e);
-        if (r != cudaSuccess) return r;
-        A->ev.push_back(e);
-    }
-    return cudaSuccess;
-}
-
-float adj_elapsed(const jlb_adjoint *A, size_t i, size_t j) {
-    float ms = 0.f;
-    cudaEventElapsedTime(&ms, A->ev[i], A->ev[j]);
-    return ms;
-}
-
-// relaxation rates of relaxation time tau (jyulb/isothermal.pyx:274-287)
-void adj_rates(const jlb_adjoint *A, double tau, double &we, double &wo) {
-    we = 1.0 / tau;
-    wo = we;
-    if (A->s->cfg.rlx_scheme == JLB_TRT)
-        wo = A->magic > 0.0 ? 1.0 / (A->magic / (tau - 0.5) + 0.5) : 8.0 * (2.0 - we) / (8.0 - we);
-}
-
-} // namespace
-
-extern "C" {
-
-void jlb_adj_destroy(jlb_adjoint *A) {
-    if (!A) return;
-    if (A->s) cudaStreamSynchronize(A->s->st);
-    if (A->st2) { cudaStreamSynchronize(A->st2); cudaStreamDestroy(A->st2); }
-    for (void *p : A->ckpt) if (p) cudaFree(p);
-    for (void *p : A->snap) if (p) cudaFree(p);
-    for (cudaEvent_t e : A->ev) cudaEventDestroy(e);
-    void *bufs[] = {A->f0, A->lam, A->sp_in, A->d_target, A->d_part, A->d_guin};
-    for (void *p : bufs) if (p) cudaFree(p);
-    if (A->s) jlb_destroy(A->s);
-    delete A;
-}
-
-int jlb_adj_create(const jlb_config *cfg, const uint8_t *phase, int32_t loss_plane, int32_t checkpoint_every,
-                   jlb_adjoint **out) {
-    jlb_adjoint *A = nullptr;
-    if (!cfg || !phase || !out) return afail(nullptr, JLB_ERR_INVALID_ARG, "NULL argument");
-    *out = nullptr;
-    if (cfg->precision == JLB_FP16) return afail(nullptr, JLB_ERR_UNSUPPORTED, "adjoint supports FP64 and FP32");
-    if (checkpoint_every < 1) return afail(nullptr, JLB_ERR_INVALID_ARG, "checkpoint interval must be >= 1");
-    if (cfg->kernel != JLB_KERNEL_JYULB)
-        return afail(nullptr, JLB_ERR_UNSUPPORTED, "adjoint supports the jyulb collision kernel");
-    for (int f = 1; f < 6; ++f)
-        if (cfg->bc[f] == JLB_FIXED_VEL)
-            return afail(nullptr, JLB_ERR_UNSUPPORTED, "adjoint: FIXED_VEL is supported on face 1X only");
-    if (cfg->bc[0] == JLB_FIXED_VEL && cfg->bc[1] != JLB_PERIODIC && cfg->lat_size[0] == 1)
-        return afail(nullptr, JLB_ERR_UNSUPPORTED, "adjoint: a one-site-thick domain with two Zou-He faces");
-    if (loss_plane < 0 || loss_plane >= cfg->lat_size[0]) return afail(nullptr, JLB_ERR_INVALID_ARG, "loss plane out of range");
-    A = new jlb_adjoint();
-    A->K = checkpoint_every;
-    A->plane = loss_plane;
-    A->magic = cfg->trt_magic;
-    int r = jlb_create(cfg, &A->s);
-    if (r) { std::string m = g_create_error; delete A; return afail(nullptr, r, m); }
-    jlb_solver *s = A->s;
-    s->no_sparse = true;  // checkpoints and recomputation work on the lattice layout
-    s->no_lin = true;
-    // rest state: den = 1, vel = 0 everywhere, so the initial populations do
-    // not depend on the parameters
-    std::vector<uint8_t> ph((size_t)s->NCNT, 0);
-    std::vector<double> den((size_t)s->NCNT, 1.0), vel(3 * (size_t)s->NCNT, 0.0);
-    for (int i = 0; i < s->nx; ++i)
-        for (int j = 0; j < s->ny; ++j)
-            for (int k = 0; k < s->nz; ++k)
-                ph[fidx(s, i + 1, j + 1, k + 1)] = phase[((size_t)i * s->ny + j) * s->nz + k];
-    uint64_t nf = 0;
-    if ((r = jlb_finalize_init(s, ph.data(), den.data(), vel.data(), &nf))) {
-        std::string m = s->err;
-        jlb_adj_destroy(A);
-        return afail(nullptr, r, m);
-    }
-    A->fbytes = (size_t)19 * s->Np * s->ssz;
-    auto bail = [&](const char *m) { jlb_adj_destroy(A); return afail(nullptr, JLB_ERR_NOMEM, m); };
-    if (cudaMalloc(&A->f0, A->fbytes) != cudaSuccess || cudaMalloc(&A->lam, A->fbytes) != cudaSuccess ||
-        cudaMalloc(&A->d_target, 3 * sizeof(double) * (size_t)s->ny * s->nz) != cudaSuccess ||
-        cudaMalloc(&A->d_guin, sizeof(double) * (size_t)s->ny * s->nz) != cudaSuccess) {
-        cudaGetLastError();
-        return bail("adjoint state allocation failed");
-    }
-    A->nparts = adjoint_blocks(make_args(s, 0));
-    if (cudaMalloc(&A->d_part, 5 * sizeof(double) * (size_t)A->nparts) != cudaSuccess ||
-        (s->M > 0 && cudaMalloc(&A->sp_in, (size_t)2 * A->K * 19 * s->M * s->ssz) != cudaSuccess) ||
-        cudaStreamCreateWithFlags(&A->st2, cudaStreamNonBlocking) != cudaSuccess) {
-        cudaGetLastError();
-        return bail("adjoint state allocation failed");
-    }
-    cudaMemcpy(A->f0, s->f, A->fbytes, cudaMemcpyDeviceToDevice);
-    *out = A;
-    return JLB_OK;
-}
-
-int jlb_adj_forward(jlb_adjoint *A, double tau, const double g[3], const double *uin, double rho_out, uint32_t steps,
-                    const double *target, double *loss, double *u_plane) {
-    if (!A || !g || !uin || steps < 1) return afail(A, JLB_ERR_INVALID_ARG, "bad argument");
-    if (!(tau > 0.5)) return afail(A, JLB_ERR_INVALID_ARG, "tau must exceed 1/2");
-    jlb_solver *s = A->s;
-    double we, wo;
-    adj_rates(A, tau, we, wo);
-    s->we = we;
-    s->wo = wo;
-    for (int d = 0; d < 3; ++d) s->g[d] = g[d];
-    ++s->args_version;
-    // Zou-He data: inlet 1X velocity (uin[j*nz+k], 0, 0), outlet density rho_out
-    const int M = s->M;
-    const size_t nb = 4 * (size_t)std::max(s->bc_slots, 1) * M;
-    std::vector<double> bc(nb, 0.0);
-    for (int t = 0; t < M; ++t) {
-        const int64_t n = s->sp_node[t];
-        const int j = (int)((n / s->nz) % s->ny), k = (int)(n % s->nz);
-        const uint32_t faces = (s->sp_info[t] >> SP_FACE_SHIFT) & 0x3Fu;
-        int slot = 0;
-        for (int face = 0; face < 6; ++face) {
-            if (!(faces & (1u << face))) continue;
-            const bool vel_face = s->cfg.bc[face] == JLB_FIXED_VEL;
-            bc[(size_t)(4 * slot) * M + t] = vel_face ? 1.0 : rho_out;
-            bc[(size_t)(4 * slot + 1) * M + t] = vel_face ? uin[(size_t)j * s->nz + k] : 0.0;
-            slot = 1;
-        }
-    }
-    if (M > 0) {
-        ACK(cudaMemcpyAsync(s->d_sp_bc, bc.data(), nb * sizeof(double), cudaMemcpyHostToDevice, s->st));
-        ACK(cudaMemsetAsync(s->d_sp_den, 0, (size_t)M * s->csz, s->st));
-    }
-    // forward with checkpoints
-    ACK(adj_events(A, 2));
-    ACK(cudaEventRecord(A->ev[0], s->st));
-    ACK(cudaMemcpyAsync(s->f, A->f0, A->fbytes, cudaMemcpyDeviceToDevice, s->st));
-    s->parity = 0;
-    const int nseg = (int)((steps + A->K - 1) / A->K);
-    while ((int)A->ckpt.size() < nseg) {
-        void *p = nullptr;
-        ACK(cudaMalloc(&p, A->fbytes));
-        A->ckpt.push_back(p);
-    }
-    for (int seg = 0; seg < nseg; ++seg) {
-        ACK(cudaMemcpyAsync(A->ckpt[seg], s->f, A->fbytes, cudaMemcpyDeviceToDevice, s->st));
-        const uint32_t t0 = (uint32_t)seg * A->K, t1 = std::min<uint32_t>(steps, t0 + A->K);
-        int r = run_steps(s, t1 - t0, t1 == steps);
-        if (r) return afail(A, r, s->err);
-    }
-    ACK(cudaEventRecord(A->ev[1], s->st));
-    // stored velocity on the loss plane, and the loss
-    const size_t plane_n = (size_t)s->ny * s->nz;
-    const int64_t p0 = (int64_t)A->plane * s->ny * s->nz;
-    std::vector<double> up(3 * plane_n);
-    std::vector<uint32_t> pm(plane_n);
-    ACK(cudaMemcpyAsync(pm.data(), s->nmask + p0, plane_n * 4, cudaMemcpyDeviceToHost, s->st));
-    for (int c = 0; c < 3; ++c) {
-        if (s->prec == PREC_FP64) {
-            ACK(cudaMemcpyAsync(up.data() + c * plane_n, (double *)s->mom[1 + c] + p0, plane_n * 8,
-                                cudaMemcpyDeviceToHost, s->st));
-        } else {
-            std::vector<float> tmp(plane_n);
-            ACK(cudaMemcpyAsync(tmp.data(), (float *)s->mom[1 + c] + p0, plane_n * 4, cudaMemcpyDeviceToHost, s->st));
-            ACK(cudaStreamSynchronize(s->st));
-            for (size_t m = 0; m < plane_n; ++m) up[c * plane_n + m] = tmp[m];
-        }
-    }
-    ACK(cudaStreamSynchronize(s->st));
-    A->ms[0] = adj_elapsed(A, 0, 1);
-    double L = 0.0;
-    for (size_t m = 0; m < plane_n; ++m) {
-        if (pm[m] & MASK_SOLID) continue;
-        for (int c = 0; c < 3; ++c) {
-            const double u = up[c * plane_n + m];
-            if (u_plane) u_plane[3 * m + c] = u;
-            if (target) { const double d = u - target[3 * m + c]; L += d * d; }
-        }
-    }
-    std::vector<double> tg(3 * plane_n, 0.0);
-    if (target)
-        for (size_t m = 0; m < plane_n; ++m)
-            if (!(pm[m] & MASK_SOLID)) for (int c = 0; c < 3; ++c) tg[3 * m + c] = target[3 * m + c];
-    ACK(cudaMemcpy(A->d_target, tg.data(), tg.size() * sizeof(double), cudaMemcpyHostToDevice));
-    if (loss) *loss = L;
-    A->steps = steps;
-    A->tau = tau;
-    A->have_forward = true;
-    return JLB_OK;
-}
-
-int jlb_adj_backward(jlb_adjoint *A, double *dtau, double dg[3], double *duin) {
-    if (!A) return afail(A, JLB_ERR_INVALID_ARG, "NULL adjoint");
-    if (!A->have_forward) return afail(A, JLB_ERR_STATE, "run jlb_adj_forward first");
-    jlb_solver *s = A->s;
-    const uint32_t steps = A->steps;
-    const int K = A->K;
-    const int nseg = (int)((steps + K - 1) / K);
-    // one buffer set, a second when memory allows (and there is a next segment)
-    const int want = nseg > 1 ? 2 : 1;
-    while (A->nsets < want) {
-        std::vector<void *> set;
-        bool ok = true;
-        for (int i = 0; i < K && ok; ++i) {
-            void *p = nullptr;
-            ok = cudaMalloc(&p, A->fbytes) == cudaSuccess;
-            if (ok) set.push_back(p);
-        }
-        if (!ok) {
-            cudaGetLastError();
-            for (void *p : set) cudaFree(p);
-            if (A->nsets == 0) return afail(A, JLB_ERR_NOMEM, "adjoint recompute buffers");
-            break;
-        }
-        A->snap.insert(A->snap.end(), set.begin(), set.end());
-        ++A->nsets;
-    }
-    const int nsets = std::min(A->nsets, want);
-    ACK(adj_events(A, 4 + 4 * (size_t)nseg));
-    cudaEvent_t *ev = A->ev.data();
-    cudaStream_t st = s->st, st2 = A->st2;
-    ACK(cudaEventRecord(ev[2], st));
-    ACK(cudaMemsetAsync(A->lam, 0, A->fbytes, st));
-    ACK(cudaMemsetAsync(A->d_part, 0, 5 * sizeof(double) * (size_t)A->nparts, st));
-    ACK(cudaMemsetAsync(A->d_guin, 0, sizeof(double) * (size_t)s->ny * s->nz, st));
-    ACK(cudaStreamWaitEvent(st2, ev[2], 0)); // checkpoints of the forward run are complete
-    const size_t sp_step = (size_t)19 * s->M * s->ssz; // bytes of one step's boundary-site inputs
-    auto seg_ev = [&](int seg) { return ev + 4 + 4 * (size_t)seg; }; // rc start, rc end, rv start, rv end
-    auto range = [&](int seg, uint32_t &t0, uint32_t &t1) {
-        t0 = (uint32_t)seg * K;
-        t1 = std::min<uint32_t>(steps, t0 + K);
-    };
-    auto state_before = [&](int seg, uint32_t t) -> void * {
-        const uint32_t t0 = (uint32_t)seg * K;
-        return t == t0 ? A->ckpt[seg] : A->snap[(size_t)(seg % nsets) * K + (t - t0)];
-    };
-    auto sp_in_of = [&](int seg, uint32_t t) -> void * {
-        if (s->M == 0) return nullptr;
-        return (char *)A->sp_in + ((size_t)(seg % nsets) * K + (t - (uint32_t)seg * K)) * sp_step;
-    };
-    // recompute a segment out of place on st2; its last step's outputs are not
-    // needed, so that step runs the boundary sites only (into the scratch slot)
-    auto recompute = [&](int seg) -> int {
-        uint32_t t0, t1;
-        range(seg, t0, t1);
-        ACK(cudaEventRecord(seg_ev(seg)[0], st2));
-        for (uint32_t t = t0; t < t1; ++t) {
-            StepArgs a = make_args(s, 0);
-            a.f = state_before(seg, t);
-            a.fout = t + 1 < t1 ? state_before(seg, t + 1) : A->snap[(size_t)(seg % nsets) * K];
-            a.sp_tee = sp_in_of(seg, t);
-            if (t + 1 == t1) a.nb_dense = 0;
-            if (a.nb_dense == 0 && a.M == 0) continue;
-            const int blocks = a.nb_dense + (a.M + 127) / 128;
-            const bool pstep = (t & 1u) == 0;
-            const int r = s->prec == PREC_FP64 ? launch_step_fp64(a, s->cfg.rlx_scheme, pstep, s->accf, blocks, st2)
-                                               : launch_step_fp32(a, s->cfg.rlx_scheme, pstep, s->accf, blocks, st2);
-            if (r) return afail(A, JLB_ERR_CUDA, std::string("recompute step: ") + cudaGetErrorString((cudaError_t)r));
-            ++s->launches;
-        }
-        ACK(cudaEventRecord(seg_ev(seg)[1], st2));
-        return JLB_OK;
-    };
-    int r = recompute(nseg - 1);
-    if (r) return r;
-    for (int seg = nseg - 1; seg >= 0; --seg) {
-        uint32_t t0, t1;
-        range(seg, t0, t1);
-        ACK(cudaStreamWaitEvent(st, seg_ev(seg)[1], 0));
-        ACK(cudaEventRecord(seg_ev(seg)[2], st));
-        for (int64_t t = (int64_t)t1 - 1; t >= (int64_t)t0; --t) {
-            AdjArgs a{};
-            a.s = make_args(s, 0);
-            a.snap = state_before(seg, (uint32_t)t);
-            a.sp_in = sp_in_of(seg, (uint32_t)t);
-            a.lam = A->lam;
-            a.seed = (uint32_t)t == steps - 1;
-            a.plane = A->plane;
-            a.target = A->d_target;
-            a.part = A->d_part;
-            a.grad_uin = A->d_guin;
-            r = launch_adjoint_step(a, s->prec, s->cfg.rlx_scheme, (t & 1) == 0, st);
-            if (r) return afail(A, JLB_ERR_CUDA, std::string("adjoint step: ") + cudaGetErrorString((cudaError_t)r));
-            s->launches += 2;
-        }
-        ACK(cudaEventRecord(seg_ev(seg)[3], st));
-        if (seg > 0) {
-            // the buffer set of segment seg-1 was last read by the sweep of
-            // segment seg-1+nsets
-            if (seg - 1 + nsets < nseg) ACK(cudaStreamWaitEvent(st2, seg_ev(seg - 1 + nsets)[3], 0));
-            if ((r = recompute(seg - 1))) return r;
-        }
-    }
-    ACK(cudaEventRecord(ev[3], st));
-    std::vector<double> part(5 * (size_t)A->nparts);
-    ACK(cudaMemcpyAsync(part.data(), A->d_part, part.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
-    if (duin) ACK(cudaMemcpyAsync(duin, A->d_guin, sizeof(double) * (size_t)s->ny * s->nz, cudaMemcpyDeviceToHost, st));
-    ACK(cudaStreamSynchronize(st));
-    double gr[5] = {0, 0, 0, 0, 0};
-    for (int b = 0; b < A->nparts; ++b)
-        for (int c = 0; c < 5; ++c) gr[c] += part[5 * (size_t)b + c];
-    A->ms[1] = A->ms[2] = 0.0;
-    for (int seg = 0; seg < nseg; ++seg) {
-        A->ms[1] += adj_elapsed(A, 4 + 4 * (size_t)seg, 5 + 4 * (size_t)seg);
-        A->ms[2] += adj_elapsed(A, 6 + 4 * (size_t)seg, 7 + 4 * (size_t)seg);
-    }
-    A->ms[3] = adj_elapsed(A, 2, 3);
-    // chain rule to tau: we = 1/tau, wo(tau) from the magic parameter
-    double we, wo;
-    adj_rates(A, A->tau, we, wo);
-    double dwo_dtau = 0.0;
-    if (s->cfg.rlx_scheme == JLB_TRT) {
-        const double magic = A->magic > 0.0 ? A->magic : 3.0 / 16.0;
-        dwo_dtau = wo * wo * magic / ((A->tau - 0.5) * (A->tau - 0.5));
-    }
-    if (dtau) {
-        if (s->cfg.rlx_scheme == JLB_TRT) *dtau = gr[0] * (-we * we) + gr[1] * dwo_dtau;
-        else *dtau = (gr[0] + gr[1]) * (-we * we);
-    }
-    if (dg) for (int d = 0; d < 3; ++d) dg[d] = gr[2 + d];
-    return JLB_OK;
-}
-
-int jlb_adj_timers(const jlb_adjoint *A, double out[4]) {
-    if (!A || !out) return JLB_ERR_INVALID_ARG;
-    for (int i = 0; i < 4; ++i) out[i] = A->ms[i];
-    return JLB_OK;
-}
-
-const char *jlb_adj_last_error(const jlb_adjoint *A) { return A ? A->err.c_str() : g_create_error.c_str(); }
 
 } // extern "C"
