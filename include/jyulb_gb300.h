@@ -135,7 +135,9 @@ int jlb_set_acc(jlb_solver *s, const double *acc);
  * synchronisation, no host arrays.  write_moments != 0 stores den/vel of the
  * last step on the device (read them with jlb_download_moments).  A step
  * kernel whose bounded wait on its bulk copies ran out is reported by the
- * next jlb_evolve, jlb_download_moments or jlb_get_populations call. */
+ * next jlb_evolve, jlb_download_moments or jlb_get_populations call; the
+ * solver keeps reporting it until jlb_finalize_init or jlb_set_populations
+ * gives it a whole state again. */
 int jlb_step(jlb_solver *s, uint32_t tsteps, int write_moments);
 
 /* copies the device den/vel of the last moment-writing step into the
@@ -189,9 +191,12 @@ int jlb_flow_info(jlb_solver *s, double ref_den, double out[12]);
  * sites; larger or non-positive sizes return JLB_ERR_INVALID_ARG.  Scratch is
  * a static device array of 256 KiB that every GPU loading the library keeps
  * until the process exits; the first call on each device looks up its address
- * and should therefore come before any stream capture.  All calls share that
- * array (each call writes every partial it reads), so calls that overlap on
- * the GPU race: serialise them, e.g. on one stream. */
+ * and should therefore come before any stream capture (a lookup that failed is
+ * retried by the next call).  All calls share that array (each call writes
+ * every partial it reads), so calls that overlap on the GPU race: serialise
+ * them, e.g. on one stream.  The call clears the CUDA runtime's last-error
+ * slot on entry, so that an error left there by an earlier launch is not
+ * reported as its own. */
 int jlb_reduce_moments_noalloc(const uint32_t *nmask, const void *den, const void *ux, const void *uy,
                                const void *uz, int64_t n_sites, int32_t precision, double *out, void *stream);
 

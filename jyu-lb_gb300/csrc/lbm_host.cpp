@@ -1195,6 +1195,8 @@ int jlb_finalize_init(jlb_solver *s, uint8_t *phase, double *den, double *vel, u
         CK(cudaMemcpyAsync(dvel, vel, 3 * nb * sizeof(double), cudaMemcpyHostToDevice, s->st));
         CK(cudaMemsetAsync(s->f, 0, (size_t)19 * s->Np * s->ssz, s->st));
         for (int c = 0; c < 4; ++c) CK(cudaMemsetAsync(s->mom[c], 0, (size_t)s->Np * s->csz, s->st));
+        // a new state clears a timed-out wait recorded by earlier steps
+        CK(cudaMemsetAsync(s->d_err, 0, sizeof(int), s->st));
         if (s->cfg.kernel == JLB_KERNEL_CXX)
             r = aux_init_cxx(s->geom, s->cfg.rlx_scheme, s->cfg.kernel_opts, dph, dden, dvel,
                              s->accf ? (const double *)s->acc : nullptr, s->g, s->tau, s->we, s->wo, (double *)s->f,
@@ -1381,6 +1383,7 @@ int jlb_set_populations(jlb_solver *s, const double *f) {
     CK(cudaMalloc(&tmp, nb));
     cudaError_t e = cudaMemcpyAsync(tmp, f, nb, cudaMemcpyHostToDevice, s->st);
     if (e == cudaSuccess) e = (cudaError_t)aux_restore(s->prec, s->geom, s->f, s->nmask, tmp, s->st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(s->d_err, 0, sizeof(int), s->st); // the restored state is whole
     s->c_current = false;  // the lattice copy is current again
     ++s->launches;
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);

@@ -20,11 +20,12 @@ namespace {
 using namespace jlb;
 
 constexpr int NA_THREADS = 256;
-constexpr int64_t NA_CHUNK = 65536;     // sites summed by one block
-constexpr int NA_MAX_PARTIALS = 4096;   // blocks, so at most 2^28 sites
+constexpr int64_t NA_MAX_SITES = (int64_t)1 << 28;
+constexpr int NA_MAX_PARTIALS = 4096;   // blocks of the partial-sum pass
 constexpr int NA_COMPONENTS = 8;
 
-// Partial sums of the last call: 4096 x 8 doubles = 256 KiB per device.
+// Partial sums of the last call: at most 4096 x 8 doubles = 256 KiB per
+// device.
 static __device__ __align__(256) double g_noalloc_scratch[NA_MAX_PARTIALS * NA_COMPONENTS];
 
 template <class C, bool SHIFTED>
@@ -32,10 +33,9 @@ __global__ void __launch_bounds__(NA_THREADS) noalloc_partial_kernel(const uint3
                                                                      const C *ux, const C *uy, const C *uz,
                                                                      int64_t n_sites, double *partial) {
     double acc[NA_COMPONENTS] = {0, 0, 0, 0, 0, 0, 0, 0};
-    const int64_t lo = (int64_t)blockIdx.x * NA_CHUNK;
-    int64_t hi = lo + NA_CHUNK;
-    if (hi > n_sites) hi = n_sites;
-    for (int64_t n = lo + threadIdx.x; n < hi; n += NA_THREADS) {
+    // grid-stride: the grid is sized to the GPU, not to the input
+    const int64_t stride = (int64_t)gridDim.x * NA_THREADS;
+    for (int64_t n = (int64_t)blockIdx.x * NA_THREADS + threadIdx.x; n < n_sites; n += stride) {
         if (nmask[n] & MASK_SOLID) continue;
         const double d = SHIFTED ? 1.0 + (double)den[n] : (double)den[n];
         const double u0 = (double)ux[n], u1 = (double)uy[n], u2 = (double)uz[n];
@@ -73,11 +73,36 @@ __global__ void noalloc_final_kernel(const double *partial, int nblocks, double 
     if (lane == 0) out[c] = v;
 }
 
-// device address of the static scratch, looked up once per device
+// device address of the static scratch and the SM count, per device; a
+// lookup is kept only once it succeeded (a failed one, e.g. under stream
+// capture, is retried by the next call)
 constexpr int NA_MAX_DEVICES = 64;
-std::once_flag g_once[NA_MAX_DEVICES];
+std::mutex g_mu;
 double *g_scratch_ptr[NA_MAX_DEVICES] = {nullptr};
-cudaError_t g_scratch_err[NA_MAX_DEVICES] = {cudaSuccess};
+int g_sms[NA_MAX_DEVICES] = {0};
+
+bool scratch_of(int dev, double *&ptr, int &sms) {
+    std::lock_guard<std::mutex> lock(g_mu);
+    if (!g_scratch_ptr[dev]) {
+        // the host name of g_noalloc_scratch is only a stand-in for the
+        // device array: resolve its device address with this device current
+        void *p = nullptr;
+        if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) {
+            cudaGetLastError(); // leave no error of the failed lookup behind
+            return false;
+        }
+        int n = 0;
+        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+            cudaGetLastError();
+            n = 0;
+        }
+        g_sms[dev] = n > 0 ? n : 1;
+        g_scratch_ptr[dev] = (double *)p;
+    }
+    ptr = g_scratch_ptr[dev];
+    sms = g_sms[dev];
+    return true;
+}
 
 } // namespace
 
@@ -85,21 +110,23 @@ extern "C" int jlb_reduce_moments_noalloc(const uint32_t *nmask, const void *den
                                           const void *uz, int64_t n_sites, int32_t precision, double *out,
                                           void *stream) {
     if (!nmask || !den || !ux || !uy || !uz || !out) return JLB_ERR_INVALID_ARG;
-    if (n_sites < 1 || n_sites > (int64_t)NA_MAX_PARTIALS * NA_CHUNK) return JLB_ERR_INVALID_ARG;
+    if (n_sites < 1 || n_sites > NA_MAX_SITES) return JLB_ERR_INVALID_ARG;
     if (precision != JLB_FP64 && precision != JLB_FP32 && precision != JLB_FP16) return JLB_ERR_INVALID_ARG;
+    // an error left in the runtime's last-error slot by an earlier, unrelated
+    // launch is not this call's failure
+    cudaGetLastError();
     int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess) return JLB_ERR_CUDA;
+    if (cudaGetDevice(&dev) != cudaSuccess) { cudaGetLastError(); return JLB_ERR_CUDA; }
     if (dev < 0 || dev >= NA_MAX_DEVICES) return JLB_ERR_UNSUPPORTED;
-    // the host name of g_noalloc_scratch is only a stand-in for the device
-    // array: resolve its device address with this device current
-    std::call_once(g_once[dev], [dev] {
-        void *p = nullptr;
-        g_scratch_err[dev] = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        g_scratch_ptr[dev] = (double *)p;
-    });
-    if (g_scratch_err[dev] != cudaSuccess || !g_scratch_ptr[dev]) return JLB_ERR_CUDA;
-    double *partial = g_scratch_ptr[dev];
-    const int nblocks = (int)((n_sites + NA_CHUNK - 1) / NA_CHUNK);
+    double *partial = nullptr;
+    int sms = 1;
+    if (!scratch_of(dev, partial, sms)) return JLB_ERR_CUDA;
+    // four blocks per SM, fewer for inputs of fewer sites than that covers
+    int64_t nb = 4 * (int64_t)sms;
+    const int64_t need = (n_sites + NA_THREADS - 1) / NA_THREADS;
+    if (nb > need) nb = need;
+    if (nb > NA_MAX_PARTIALS) nb = NA_MAX_PARTIALS;
+    const int nblocks = (int)nb;
     cudaStream_t st = (cudaStream_t)stream;
     if (precision == JLB_FP64)
         noalloc_partial_kernel<double, false><<<nblocks, NA_THREADS, 0, st>>>(
@@ -109,6 +136,7 @@ extern "C" int jlb_reduce_moments_noalloc(const uint32_t *nmask, const void *den
         noalloc_partial_kernel<float, true><<<nblocks, NA_THREADS, 0, st>>>(
             nmask, (const float *)den, (const float *)ux, (const float *)uy, (const float *)uz, n_sites,
             partial);
+    if (cudaGetLastError() != cudaSuccess) return JLB_ERR_CUDA;
     noalloc_final_kernel<<<1, 256, 0, st>>>(partial, nblocks, out);
     return cudaGetLastError() == cudaSuccess ? JLB_OK : JLB_ERR_CUDA;
 }

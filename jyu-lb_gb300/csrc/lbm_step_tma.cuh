@@ -151,7 +151,9 @@ __global__ void __launch_bounds__(128, JLB_MIN_BLOCKS_TMA) lbm_step_tma_kernel(c
         if (__syncthreads_or(!ok)) {
             if (t == 0) {
                 atomicExch(err, 1);
-                // let the copies this block already issued land before leaving
+                // let the copies this block already issued land before
+                // leaving: those of this tile (bounded again) and of the next
+                (void)mbar_wait_bounded(&bar[it & 1], (uint32_t)(it >> 1) & 1u);
                 if (next < ntiles) (void)mbar_wait_bounded(&bar[(it + 1) & 1], (uint32_t)((it + 1) >> 1) & 1u);
             }
             __syncthreads();

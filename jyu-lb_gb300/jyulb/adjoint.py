@@ -47,6 +47,7 @@ class ChannelProblem:
                 self._lib.jlb_adj_last_error(None).decode())
         self._h = h
         self.steps = 0
+        self.run_id = 0  # counts forward runs; backward() differentiates the last one
 
     def __del__(self):
         h = getattr(self, '_h', None)
@@ -71,6 +72,7 @@ class ChannelProblem:
                                               _native.dptr(tgt) if tgt is not None else None,
                                               ctypes.byref(loss), _native.dptr(up)))
         self.steps = int(steps)
+        self.run_id += 1
         return float(loss.value), up
 
     def backward(self):
@@ -93,19 +95,31 @@ class ChannelProblem:
 
 def loss_fn(problem, tau, g, uin, target, steps, rho_out=1.0):
     """L(tau, g, uin) as a differentiable torch scalar (torch tensors in,
-    gradients from the adjoint)."""
+    gradients from the adjoint).
+
+    The problem's backward run differentiates its latest forward run.  When
+    another forward run on the same problem came after this node's (two
+    loss_fn graphs on one problem), the backward pass first repeats this
+    node's forward run with its own inputs, so every node gets the gradients
+    of its own loss."""
     import torch
 
     class _AdjointLoss(torch.autograd.Function):
         @staticmethod
         def forward(ctx, tau_t, g_t, uin_t):
-            loss, _ = problem.forward(float(tau_t.detach().cpu()), g_t.detach().cpu().double().numpy(),
-                                      uin_t.detach().cpu().double().numpy(), steps, target, rho_out)
+            args = (float(tau_t.detach().cpu()), g_t.detach().cpu().double().numpy(),
+                    uin_t.detach().cpu().double().numpy())
+            loss, _ = problem.forward(*args, steps, target, rho_out)
             ctx.dev, ctx.dtype = tau_t.device, tau_t.dtype
+            ctx.args = args
+            ctx.run_id = problem.run_id
             return torch.tensor(loss, dtype=torch.float64, device=tau_t.device)
 
         @staticmethod
         def backward(ctx, grad_out):
+            if problem.run_id != ctx.run_id:
+                problem.forward(*ctx.args, steps, target, rho_out)
+                ctx.run_id = problem.run_id
             dtau, dg, duin = problem.backward()
             s = float(grad_out)
             return (torch.tensor(s * dtau, dtype=torch.float64, device=ctx.dev),

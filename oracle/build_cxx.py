@@ -22,7 +22,9 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
 EXE = os.path.join(OUT, "jyu_lb_isothermal")
-REF = os.environ.get("JYULB_REFERENCE_ROOT", "/root/reference")
+# the reference checkout: JYULB_REFERENCE_ROOT, else a directory named
+# "reference" beside this repository
+REF = os.environ.get("JYULB_REFERENCE_ROOT") or os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")
 SOURCES = ["source/isothermal/jyu_lb_isothermal.cpp", "include/common/node.cpp", "include/common/filter.cpp",
            "include/collision/collision.cpp", "include/kernel/kernel.cpp", "include/solver/solver.cpp",
            "include/io/input_parser.cpp", "include/io/raw_io.cpp"]

@@ -34,7 +34,12 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
 SRC_OUT = os.path.join(OUT, "src")
 PKG_OUT = os.path.join(OUT, "jyulb")
-REF_PKG = os.environ.get("JYULB_REFERENCE_PKG", "/root/reference/jyulb")
+# the reference's jyulb package: JYULB_REFERENCE_PKG, else the jyulb folder of
+# JYULB_REFERENCE_ROOT, else of a directory named "reference" beside this
+# repository
+REF_PKG = os.environ.get("JYULB_REFERENCE_PKG") or os.path.join(
+    os.environ.get("JYULB_REFERENCE_ROOT") or os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference"),
+    "jyulb")
 MODULES = ["defs", "bcs", "D3Q19", "isothermal", "flow_field"]
 
 

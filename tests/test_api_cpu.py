@@ -187,3 +187,41 @@ def test_bcs_zou_he_enforces_velocity_and_density(face):
     assert np.allclose(den, 1.02, atol=1e-14)
     tang = [a for a in range(3) if a != face >> 1]
     assert np.allclose(mom[tang] / 1.02, v[tang, None], atol=1e-14)
+
+
+def test_loss_fn_backward_differentiates_its_own_forward_run():
+    """Two loss_fn graphs on one problem: each backward pass must return the
+    gradients of its own loss, although the problem's backward run only
+    knows the latest forward run.  A stand-in problem (no GPU) whose
+    gradient is the tau of the forward run it follows shows which run each
+    backward pass differentiated."""
+    torch = pytest.importorskip("torch")
+    from jyulb.adjoint import loss_fn
+
+    class FakeProblem:
+        def __init__(self):
+            self.run_id = 0
+            self.last_tau = None
+            self.forwards = 0
+
+        def forward(self, tau, g, uin, steps, target=None, rho_out=1.0):
+            self.run_id += 1
+            self.forwards += 1
+            self.last_tau = tau
+            return tau * tau, None
+
+        def backward(self):
+            return 2.0 * self.last_tau, np.zeros(3), np.zeros((2, 2))
+
+    p = FakeProblem()
+    g, uin = torch.zeros(3, dtype=torch.float64), torch.zeros(2, 2, dtype=torch.float64)
+    t1 = torch.tensor(0.6, dtype=torch.float64, requires_grad=True)
+    t2 = torch.tensor(0.9, dtype=torch.float64, requires_grad=True)
+    l1 = loss_fn(p, t1, g, uin, None, 10)
+    l2 = loss_fn(p, t2, g, uin, None, 10)
+    l1.backward()  # the problem's latest forward run is l2's
+    assert abs(float(t1.grad) - 1.2) < 1e-15
+    assert p.forwards == 3  # l1's forward run was repeated once
+    l2.backward()
+    assert abs(float(t2.grad) - 1.8) < 1e-15
+    assert p.forwards == 4

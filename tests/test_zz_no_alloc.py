@@ -25,7 +25,7 @@ def _ptr(t):
     return ctypes.c_void_p(t.data_ptr())
 
 
-@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("precision", [0, 1, 2])
 def test_noalloc_reduce_matches_jlb_reduce(precision):
     import torch
 
@@ -51,8 +51,8 @@ def test_noalloc_reduce_matches_jlb_reduce(precision):
             cols = [den, vel[:, 0], vel[:, 1], vel[:, 2]]
             tens = [torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in cols]
         else:
-            # the FP32 solver keeps den - 1 and u in float32; these
-            # conversions recover its device values exactly
+            # the FP32 and FP16-storage solvers keep den - 1 and u in
+            # float32; these conversions recover their device values exactly
             cols = [den - 1.0, vel[:, 0], vel[:, 1], vel[:, 2]]
             tens = [torch.from_numpy(np.ascontiguousarray(a, dtype=np.float32)).cuda() for a in cols]
         out.fill_(-1.0)
