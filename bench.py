@@ -16,8 +16,17 @@ Our arm (default) prints one JSON line with
   fp64         the same for the FP64 plain path (304 B per site);
   fp16         the same for FP16 storage with FP32 arithmetic (76 B per site);
   error        relative L2 velocity errors of FP32 and FP16 against FP64 after
-               --err-steps steps of the same cavity;
-  cpu_baseline the reference's own OpenMP solver on this host's cores.
+               --err-steps (10000) steps of the same cavity;
+  cpu_baseline the reference's own OpenMP solver on this host's cores;
+  porous       the 384x256x256 regularized porous channel: FP64 / FP32 / FP16
+               MLUPS and roofline over 5000 steps, Darcy flux error vs FP64;
+  ensemble     512 channels in one launch per step: MLUPS, roofline, error of
+               sampled domains vs FP64 single-domain runs after 2000 steps;
+  adjoint      the 256x64x64 inverse problem: backward/forward device-time
+               ratio over 2000 steps (checkpoints every 50), reverse-sweep
+               roofline, gradients vs central differences of the FP64 model.
+The three workload blocks run on one GPU only (--blocks none skips them);
+each has its own clocks, roofline and error.
 `--impl reference` times only the reference's CPU solver on the same config.
 Inputs (1.3 GB of FP32 populations) exceed the 129 MB L2, so no flush is used.
 """
@@ -314,7 +323,10 @@ def ensemble_domains(n, seed=2024, scale=1.0):
     return doms
 
 
-def run_ensemble(args):
+def ensemble_block(args):
+    """The batched ensemble: `--ens-steps` steps in all (a few untimed
+    warm-up steps, the rest timed with CUDA events), then a sample of domains
+    re-run as FP64 single domains for the same number of steps."""
     import torch
     from jyulb.defs import BGK, FP64
     from jyulb.ensemble import Ensemble
@@ -323,24 +335,31 @@ def run_ensemble(args):
     torch.cuda.set_device(0)
     t0 = time.perf_counter()
     doms = ensemble_domains(args.domains)
-    ens = Ensemble(doms, BGK)
+    st = torch.cuda.Stream()
+    ens = Ensemble(doms, BGK, stream=st.cuda_stream)
     setup_s = time.perf_counter() - t0
     info = ens.info()
     nf = info["fluid_sites"]
-    ens.evolve(args.warmup)
+    total = max(args.ens_steps, args.warmup + 1)
+    warm = min(args.warmup, total - 1)
+    steps = total - warm
+    ens.evolve(warm)
     torch.cuda.synchronize()
     l0 = ens.info()["launches"]
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(0) as clk:
-        t0 = time.perf_counter()
-        ens.evolve(args.steps)
+        w0 = time.time()
+        e0.record(st)
+        ens.evolve(steps)
+        e1.record(st)
         torch.cuda.synchronize()
-        dt = time.perf_counter() - t0
+        window = (w0, time.time())
+    dt = e0.elapsed_time(e1) * 1e-3
     launches = ens.info()["launches"] - l0
-    mlups = nf * args.steps / dt / 1e6
+    mlups = nf * steps / dt / 1e6
     # per-domain check: FP64 single-domain runs of a sample of domains, same
     # total step count
     errs = []
-    total = args.warmup + args.steps
     sample = range(0, len(doms), max(1, len(doms) // max(1, args.check_domains)))[: args.check_domains]
     for d in sample:
         dom = doms[d]
@@ -355,24 +374,32 @@ def run_ensemble(args):
         v64 = np.asarray(s.get_vel())
         errs.append(float(np.linalg.norm(v[fl] - v64[fl]) / np.linalg.norm(v64[fl])))
         del s
+    del ens
+    torch.cuda.empty_cache()
     peak, peak_kind = measured_peak()
-    ach = nf * BYTES_FP32 / (dt / args.steps) / 1e9
-    line = {
+    ach = nf * BYTES_FP32 / (dt / steps) / 1e9
+    return {
         "metric": "D3Q19 MLUPS, batched ensemble of channels (FP32 shifted, one launch per step)",
-        "value": round(mlups, 3), "unit": "MLUPS", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": round(dt * 1e3 / args.steps, 4), "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "value": round(mlups, 3), "unit": "MLUPS", "steps": steps, "warmup": warm,
+        "ms_per_step": round(dt * 1e3 / steps, 4), "dtype": "f32",
         "config": {"workload": f"{len(doms)} channels nx~U[32,256] ny~U[16,128] nz~U[8,64], tau~U[0.55,1.5], "
                                "gx~U[1e-7,1e-5], half with moving top wall u~U[0.01,0.05]; BGK",
                    "domains": len(doms), "packed_sites": info["sites"], "fluid_sites": nf,
                    "setup_s": round(setup_s, 1), "autotuned_block": info["block"],
-                   "autotune_us_per_step": info["tune_us_per_step"]},
+                   "autotune_us_per_step": info["tune_us_per_step"],
+                   "l2_policy": "no flush: 14.5 GB of FP32 populations against the 129 MB L2"},
         "roofline": {"bound": "hbm", "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(ach / peak, 4), "peak_kind": peak_kind, "bytes_per_site": BYTES_FP32},
         "error": {"domains_checked": len(errs), "vel_rel_l2_vs_fp64_max": max(errs) if errs else None,
                   "vel_rel_l2_vs_fp64_median": statistics.median(errs) if errs else None, "steps": total},
-        "gpu_launches": launches, "clocks": clk.summary(),
+        "gpu_launches": launches, "clocks": clk.summary(window),
     }
+
+
+def run_ensemble(args):
+    line = ensemble_block(args)
+    line.update({"n_gpus": 1, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                 "data": "synthetic"})
     print(json.dumps(line))
     return 0
 
@@ -411,7 +438,7 @@ def porous_geometry(seed=2025, shape=POROUS_SHAPE, r=8, porosity=0.6):
     return phase, float(phase.mean())
 
 
-def run_porous(args):
+def porous_block(args):
     """Porous channel: FP64, FP32-shifted and FP16-storage runs of the same
     steps; MLUPS, roofline and the Darcy flux error against FP64."""
     import torch
@@ -440,11 +467,13 @@ def run_porous(args):
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         with ClockSampler(0) as clk:
+            w0 = time.time()
             e0.record(st)
             assert lib.jlb_step(h, steps - 1, 0) == 0
             assert lib.jlb_step(h, 1, 1) == 0
             e1.record(st)
             torch.cuda.synchronize()
+            window = (w0, time.time())
         ms = e0.elapsed_time(e1)
         red = s.reduce()
         assert lib.jlb_download_moments(h, s.den.ctypes.data_as(lib.jlb_download_moments.argtypes[1]),
@@ -453,8 +482,9 @@ def run_porous(args):
         ach = nf * bps / (ms * 1e-3 / steps) / 1e9
         res[name] = {"mlups": round(nf * steps / (ms * 1e-3) / 1e6, 1), "ms_per_step": round(ms / steps, 4),
                      "bytes_per_site": bps, "achieved_gbs": round(ach, 1), "roofline_frac": round(ach / peak, 4),
-                     "darcy_flux": red["vel_sum"][0] / nsites, "clocks": clk.summary()}
+                     "darcy_flux": red["vel_sum"][0] / nsites, "clocks": clk.summary(window)}
         del s
+        torch.cuda.empty_cache()
     fl = phase != 0
     for name in ("fp32", "fp16"):
         if name not in res or "fp64" not in res:
@@ -463,11 +493,10 @@ def run_porous(args):
         res[name]["darcy_rel_err_vs_fp64"] = abs(res[name]["darcy_flux"] - d64) / abs(d64)
         res[name]["vel_rel_l2_vs_fp64"] = float(np.linalg.norm(vel[name][fl] - vel["fp64"][fl]) /
                                                 np.linalg.norm(vel["fp64"][fl]))
-    line = {
+    return {
         "metric": "D3Q19 MLUPS, porous channel 384x256x256 (regularized), FP32 shifted",
-        "value": res["fp32"]["mlups"], "unit": "MLUPS", "n_gpus": 1, "steps": steps, "warmup": 0,
-        "ms_per_step": res["fp32"]["ms_per_step"], "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "value": res["fp32"]["mlups"], "unit": "MLUPS", "steps": steps, "warmup": 0,
+        "ms_per_step": res["fp32"]["ms_per_step"], "dtype": "f32",
         "config": {"workload": f"porous channel {shape[0]}x{shape[1]}x{shape[2]}, regularized tau=0.7, gx=5e-6, seeded spheres r=8 "
                                "(jittered lattice, random order) to porosity 0.6, periodic x/z, walls at the y ends",
                    "porosity": round(por, 5), "fluid_sites": int(fl.sum()), "geometry_s": round(geom_s, 1),
@@ -476,7 +505,14 @@ def run_porous(args):
                      "frac": res["fp32"]["roofline_frac"], "peak_kind": peak_kind, "bytes_per_site": BYTES_FP32},
         "precisions": res,
         "gpu_launches": 3 * steps,
+        "clocks": res["fp32"]["clocks"],
     }
+
+
+def run_porous(args):
+    line = porous_block(args)
+    line.update({"n_gpus": 1, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                 "data": "synthetic"})
     print(json.dumps(line))
     return 0
 
@@ -519,7 +555,7 @@ def adjoint_params():
     return hidden, guess
 
 
-def run_adjoint(args):
+def adjoint_block(args):
     """Adjoint workload: forward and backward device times of the FP32
     problem, and its gradients against central differences of the FP64
     forward model."""
@@ -540,12 +576,15 @@ def run_adjoint(args):
     recs = []
     walls = []
     with ClockSampler(0) as clk:
+        w0 = time.time()
         for _ in range(args.adj_reps):
             t0 = time.perf_counter()
             L, _ = p32.forward(tau0, g0, uin0, steps, target)
             dtau, dg, duin = p32.backward()
             walls.append(time.perf_counter() - t0)
             recs.append(p32.timers())
+        window = (w0, time.time())
+    del p32
     med = {k: statistics.median(r[k] for r in recs) for k in recs[0]}
     ratio = med["backward"] / med["forward"]
     # central differences of the FP64 forward model
@@ -586,11 +625,12 @@ def run_adjoint(args):
     rec_steps = steps - (steps + K - 1) // K
     rec_ms = med["recompute"] / max(rec_steps, 1)
     bwd_bytes = nf * (BYTES_ADJ_FP32 * steps + BYTES_RECOMP_FP32 * rec_steps)
-    line = {
+    del p64
+    torch.cuda.empty_cache()
+    return {
         "metric": "adjoint backward / forward device-time ratio, D3Q19 TRT channel 256x64x64, FP32 shifted",
-        "value": round(ratio, 3), "unit": "x", "n_gpus": 1, "steps": steps, "warmup": max(1, args.warmup // 5),
-        "ms_per_step": round(med["forward"] / steps, 5), "higher_is_better": False, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "value": round(ratio, 3), "unit": "x", "steps": steps, "warmup": max(1, args.warmup // 5),
+        "ms_per_step": round(med["forward"] / steps, 5), "higher_is_better": False, "dtype": "f32",
         "config": {"workload": "channel 256x64x64, seeded cylinder r=8 along z, Zou-He u_x inlet per site, "
                                "outlet rho=1, walls y/z, TRT magic 1/4; loss |u-target|^2 on x=200, target "
                                "from hidden seeded (tau, gx, uin)",
@@ -616,8 +656,13 @@ def run_adjoint(args):
                 "jyulb.adjoint (host parameters in, gradients out)",
                 "h2d_bytes_per_step": int(8 * (uin0.size + target.size + 4)),
                 "d2h_bytes_per_step": int(8 * (uin0.size + 4 + target.size))},
-        "clocks": clk.summary(),
+        "clocks": clk.summary(window),
     }
+
+
+def run_adjoint(args):
+    line = adjoint_block(args)
+    line.update({"n_gpus": 1, "scaling": "weak", "vs_baseline": None, "data": "synthetic"})
     print(json.dumps(line))
     return 0
 
@@ -662,7 +707,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--size", type=int, default=N_DEFAULT)
-    ap.add_argument("--err-steps", type=int, default=1000)
+    ap.add_argument("--err-steps", type=int, default=10000)
     ap.add_argument("--e2e-steps", type=int, default=100)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="cavity", choices=["cavity", "ensemble", "adjoint", "porous"])
@@ -674,6 +719,9 @@ def main():
     ap.add_argument("--adj-ckpt", type=int, default=50)
     ap.add_argument("--domains", type=int, default=512)
     ap.add_argument("--check-domains", type=int, default=6)
+    ap.add_argument("--ens-steps", type=int, default=2000)
+    ap.add_argument("--blocks", default="porous,ensemble,adjoint",
+                    help="workloads added to the default (cavity) line on one GPU; 'none' for the cavity alone")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -777,6 +825,14 @@ def main():
     }
     if rank == 0 and world == 1 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(n)
+    if world == 1:
+        # the other configurations of the metric, each with its own clocks,
+        # roofline and error (one GPU only: replicas would only repeat them)
+        blocks = {"porous": porous_block, "ensemble": ensemble_block, "adjoint": adjoint_block}
+        for name in [b for b in args.blocks.split(",") if b in blocks]:
+            t0 = time.perf_counter()
+            line[name] = blocks[name](args)
+            line[name]["wall_s"] = round(time.perf_counter() - t0, 1)
     if rank == 0:
         print(json.dumps(line))
     if dist:
