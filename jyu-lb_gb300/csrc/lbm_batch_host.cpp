@@ -286,7 +286,9 @@ int jlb_batch_create(int32_t scheme, const jlb_domain *doms, int32_t ndom, void 
         double wo = we;
         if (scheme == JLB_TRT)
             wo = D.trt_magic > 0.0 ? 1.0 / (D.trt_magic / (tau_e - 0.5) + 0.5) : 8.0 * (2.0 - we) / (8.0 - we);
-        B.we = (float)we; B.wo = (float)wo;
+        double wef, wof;
+        float_exact_rates(scheme == JLB_TRT, we, wo, wef, wof);
+        B.we = (float)wef; B.wo = (float)wof;
         for (int a = 0; a < 3; ++a) { B.g[a] = (float)D.g[a]; B.uw[a] = 0.0f; }
     }
     b->ntot = off;

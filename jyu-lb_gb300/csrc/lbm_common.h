@@ -18,6 +18,7 @@
 //   (A[q][x] = incoming f_q(x)).
 #pragma once
 #include <stdint.h>
+#include <cmath>
 #include <cuda_runtime.h>
 
 namespace jlb {
@@ -63,6 +64,29 @@ inline UDiv make_udiv(uint32_t d) {
     u.s1 = l < 1 ? l : 1;
     u.s2 = l > 1 ? l - 1 : 0;
     return u;
+}
+
+// Relaxation rates for the FP32 / FP16-storage kernels: the nearest values
+// to (we, wo) on a grid 2^-p, with p as fine as the FP32 operations of the
+// collision allow exactly (1 - we, we + wo, we - wo, 1 - (we + wo)/2, and
+// (we - wo)/2).  With those exact, the relaxation passes mass and momentum
+// through with unbiased rounding only; rounded coefficients would bias them
+// by ~1e-8 of their value at every step.  scheme_trt = false uses we alone.
+inline bool f32_exact(double x) { return (double)(float)x == x; }
+inline void float_exact_rates(bool scheme_trt, double we, double wo, double &wef, double &wof) {
+    for (int p = 40; p >= 16; --p) {
+        const double q = std::ldexp(1.0, p);
+        const double a = std::nearbyint(we * q) / q;
+        const double b = scheme_trt ? std::nearbyint(wo * q) / q : a;
+        if (a <= 0.0 || b <= 0.0) continue;
+        bool ok = f32_exact(a) && f32_exact(b) && f32_exact(1.0 - a);
+        if (scheme_trt)
+            ok = ok && f32_exact(a + b) && f32_exact(a - b) && f32_exact(1.0 - 0.5 * (a + b)) &&
+                 f32_exact(0.5 * (a - b));
+        if (ok) { wef = a; wof = b; return; }
+    }
+    wef = (double)(float)we;  // not reached for rates in (0, 2)
+    wof = (double)(float)wo;
 }
 
 #ifdef __CUDACC__

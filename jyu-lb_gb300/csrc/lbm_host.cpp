@@ -562,6 +562,8 @@ StepArgs make_args(const jlb_solver *s, int write_moments) {
     a.acc = s->accf ? s->acc : nullptr;
     for (int d = 0; d < 3; ++d) a.g[d] = s->g[d];
     a.w_e = s->we; a.w_o = s->wo;
+    if (s->prec != PREC_FP64 && s->cfg.kernel == JLB_KERNEL_JYULB)
+        float_exact_rates(s->cfg.rlx_scheme == JLB_TRT, s->we, s->wo, a.w_e, a.w_o);
     a.write_moments = write_moments;
     const int nzr = ((s->nz + 31) / 32) * 32;
     a.bx = nzr >= 128 ? 128 : nzr;

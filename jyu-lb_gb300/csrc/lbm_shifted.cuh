@@ -10,6 +10,15 @@
 //   of paired populations are equal.
 // The collision returns den - 1; velocities are the reference's stored ones,
 // u = j/den + a/2.
+//
+// Conservation in FP32.  Rounding that is the same at every step adds up: a
+// relaxation that multiplies the momentum by 1 - 1e-8 per step leaves a
+// relative error near 1e-4 after 10^4 steps.  So the coefficients are exact
+// where the conserved moments pass through them: the host gives the kernels
+// relaxation rates (jlb::float_exact_rates) for which 1 - w_e and the TRT pair
+// coefficients 1 - (w_e + w_o)/2 and (w_e - w_o)/2 are exact in FP32, so the
+// pair relaxation plus the projection return the momentum and mass they were
+// given up to unbiased rounding.
 #pragma once
 #include "lbm_step.cuh"
 
@@ -37,13 +46,18 @@ struct PhysShBase {
     }
 
     // P(H) for H = (H0 (shifted), H1[3], H2[6]) added to the relaxed g
-    // (g[q] already holds the relaxed part)
+    // (g[q] already holds the relaxed part).  The first-moment weights k6 and
+    // k12 are FP32 values whose real sum 2 k6 + 8 k12 is exactly 1 (k6 is one
+    // ulp below the nearest float to 1/6): with the nearest floats the
+    // projection would return (1 + 3e-8) H1, a bias of the momentum that
+    // repeats identically every step and accumulates.
     __device__ static void project_add(const C H0, const C hx, const C hy, const C hz, const C hxx,
                                        const C hxy, const C hxz, const C hyy, const C hyz, const C hzz,
                                        C *g) {
         const C tr = hxx + hyy + hzz;
         const C A0 = fmaf(-1.5f, tr, H0);
-        const C k18 = 1.0f / 18.0f, k36 = 1.0f / 36.0f, k6 = 1.0f / 6.0f, k12 = 1.0f / 12.0f;
+        const C k18 = 1.0f / 18.0f, k36 = 1.0f / 36.0f;
+        const C k6 = 0x1.555554p-3f, k12 = 0x1.555556p-4f; // 11184810 * 2^-26, 11184811 * 2^-27
         g[9] += A0 * (1.0f / 3.0f);
         C e, o;
         e = fmaf(4.5f, hxx, A0) * k18; o = hx * k6; g[16] += e + o; g[2] += e - o;
@@ -184,7 +198,8 @@ template <int SCH> struct PhysSh : PhysShBase {
             const C c1 = 1.0f - we, c2 = 1.0f - 0.5f * we;
             const C sx = fmaf(0.5f * ax, den, jx), sy = fmaf(0.5f * ay, den, jy), sz = fmaf(0.5f * az, den, jz);
             ux = sx * inv; uy = sy * inv; uz = sz * inv;
-            const C rx = den * ux, ry = den * uy, rz = den * uz;
+            // den u = s exactly: no round trip through u
+            const C rx = sx, ry = sy, rz = sz;
             H0 = dd;
             hx = fmaf(c1, jx, fmaf(we, rx, c2 * ax * den));
             hy = fmaf(c1, jy, fmaf(we, ry, c2 * ay * den));
@@ -207,7 +222,8 @@ template <int SCH> struct PhysSh : PhysShBase {
         uz = fmaf(jz, inv, 0.5f * az);
         const C wodd = (SCH == SCH_TRT) ? wo : we;
         const C c1 = 1.0f - 0.5f * wodd, c2 = 1.0f - 0.5f * we;
-        const C sx = den * ux, sy = den * uy, sz = den * uz; // momentum incl. a/2
+        // momentum incl. a/2 (= den u), formed without the round trip through u
+        const C sx = fmaf(0.5f * ax, den, jx), sy = fmaf(0.5f * ay, den, jy), sz = fmaf(0.5f * az, den, jz);
         H0 = we * dd;
         hx = fmaf(wodd, sx, c1 * ax * den);
         hy = fmaf(wodd, sy, c1 * ay * den);
@@ -294,7 +310,8 @@ template <int SCH> struct PhysH16 : PhysSh<SCH> {
             const C c1 = 1.0f - we, c2 = 1.0f - 0.5f * we;
             const C sx = fmaf(0.5f * ax, den, jx), sy = fmaf(0.5f * ay, den, jy), sz = fmaf(0.5f * az, den, jz);
             ux = sx * inv; uy = sy * inv; uz = sz * inv;
-            const C rx = den * ux, ry = den * uy, rz = den * uz;
+            // den u = s exactly: no round trip through u
+            const C rx = sx, ry = sy, rz = sz;
             H0 = dd;
             hx = fmaf(c1, jx, fmaf(we, rx, c2 * ax * den));
             hy = fmaf(c1, jy, fmaf(we, ry, c2 * ay * den));
@@ -315,7 +332,7 @@ template <int SCH> struct PhysH16 : PhysSh<SCH> {
         uz = fmaf(jz, inv, 0.5f * az);
         const C wodd = (SCH == SCH_TRT) ? wo : we;
         const C c1 = 1.0f - 0.5f * wodd, c2 = 1.0f - 0.5f * we;
-        const C sx = den * ux, sy = den * uy, sz = den * uz;
+        const C sx = fmaf(0.5f * ax, den, jx), sy = fmaf(0.5f * ay, den, jy), sz = fmaf(0.5f * az, den, jz);
         H0 = we * dd;
         hx = fmaf(wodd, sx, c1 * ax * den);
         hy = fmaf(wodd, sy, c1 * ay * den);
