@@ -271,6 +271,19 @@ int jlb_adj_backward(jlb_adjoint *a, double *dtau, double dg[3], double *duin);
 int jlb_adj_timers(const jlb_adjoint *a, double out[4]);
 const char *jlb_adj_last_error(const jlb_adjoint *a);
 
+/* Solver.bc_data_den_face_* / bc_data_vel_face_* (jyulb/isothermal.pxd:159-171):
+ * the face layer of den (and vel) for face `face` (0..5 = 1X, X1, 1Y, Y1, 1Z,
+ * Z1) as the last jlb_evolve call read it.  Like Solver._set_bc_data
+ * (jyulb/isothermal.pyx:476-502), jlb_evolve copies the whole first or last
+ * interior layer, halo rows included, at its start (before its checks and
+ * halo rules) for the faces the reference refreshes: the fixed faces, and Z1
+ * when bc[Z1] is FIXED_DEN or bc[1Z] is FIXED_VEL (:500).  Other faces, and
+ * every face before the first call, give den = 1 and vel = 0
+ * (jyulb/isothermal.pyx:253-265).  Shapes, C order: x faces (NJ,NK), y faces
+ * (NI,NK), z faces (NI,NJ); vel adds a last axis of 3.  den or vel may be
+ * NULL.  A host copy; no device work. */
+int jlb_bc_data(const jlb_solver *s, int32_t face, double *den, double *vel);
+
 /* number of steps taken since finalize (Solver.tot_tsteps) */
 uint32_t jlb_tot_tsteps(const jlb_solver *s);
 

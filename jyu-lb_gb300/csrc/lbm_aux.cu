@@ -582,6 +582,41 @@ int aux_download_rows(int prec, const AuxGeom &g, const uint32_t *nmask, const v
     return (int)cudaGetLastError();
 }
 
+// FP64 den / vel of the fluid sites on the first and last interior layers of
+// the axes in `axes` (bit 0 x, 1 y, 2 z), written into the halo-padded host
+// arrays; one thread per site, the others return at once
+template <class C, bool SHIFTED>
+__global__ void __launch_bounds__(256) layers_kernel(AuxGeom g, unsigned axes, const uint32_t *nmask, const C *den,
+                                                    const C *ux, const C *uy, const C *uz, double *hden,
+                                                    double *hvel) {
+    const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= g.N) return;
+    const int64_t syz = (int64_t)g.ny * g.nz;
+    const int i = (int)(n / syz);
+    const int64_t r = n - (int64_t)i * syz;
+    const int j = (int)(r / g.nz), k = (int)(r - (int64_t)j * g.nz);
+    const bool on = ((axes & 1u) && (i == 0 || i == g.nx - 1)) || ((axes & 2u) && (j == 0 || j == g.ny - 1)) ||
+                    ((axes & 4u) && (k == 0 || k == g.nz - 1));
+    if (!on || (nmask[n] & MASK_SOLID)) return;
+    const int64_t fn = full_idx(g, i + 1, j + 1, k + 1);
+    hden[fn] = SHIFTED ? 1.0 + (double)den[n] : (double)den[n];
+    hvel[3 * fn] = (double)ux[n];
+    hvel[3 * fn + 1] = (double)uy[n];
+    hvel[3 * fn + 2] = (double)uz[n];
+}
+
+int aux_download_layers(int prec, const AuxGeom &g, unsigned axes, const uint32_t *nmask, const void *den,
+                        const void *ux, const void *uy, const void *uz, double *hden, double *hvel, cudaStream_t st) {
+    const unsigned b = nblk(g.N, 256);
+    if (prec == PREC_FP64)
+        layers_kernel<double, false><<<b, 256, 0, st>>>(g, axes, nmask, (const double *)den, (const double *)ux,
+                                                        (const double *)uy, (const double *)uz, hden, hvel);
+    else
+        layers_kernel<float, true><<<b, 256, 0, st>>>(g, axes, nmask, (const float *)den, (const float *)ux,
+                                                      (const float *)uy, (const float *)uz, hden, hvel);
+    return (int)cudaGetLastError();
+}
+
 int aux_download(int prec, const AuxGeom &g, const uint32_t *nmask, const void *den, const void *ux,
                  const void *uy, const void *uz, double *hden, double *hvel, cudaStream_t st) {
     return aux_download_rows(prec, g, nmask, den, ux, uy, uz, hden, hvel, 0, (int64_t)g.nx * g.ny, st);

@@ -45,6 +45,10 @@ int aux_download_rows(int prec, const AuxGeom &g, const uint32_t *nmask, const v
                       cudaStream_t st);
 int aux_download(int prec, const AuxGeom &g, const uint32_t *nmask, const void *den, const void *ux,
                  const void *uy, const void *uz, double *hden, double *hvel, cudaStream_t st);
+// fluid sites of the first and last interior layers of the axes in `axes`
+// (bit 0 x, 1 y, 2 z) only: the sources of the periodic / symmetric halo rules
+int aux_download_layers(int prec, const AuxGeom &g, unsigned axes, const uint32_t *nmask, const void *den,
+                        const void *ux, const void *uy, const void *uz, double *hden, double *hvel, cudaStream_t st);
 // interior of a device-accessible halo-padded (NI,NJ,NK,3) array -> SoA field
 int aux_acc_upload(int prec, const AuxGeom &g, const double *hacc, void *acc, cudaStream_t st);
 // initial state of the C++-executable model (lbm_cxx.cu); facc: SoA force

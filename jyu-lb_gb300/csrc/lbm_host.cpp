@@ -114,6 +114,51 @@ void enforce_phase(const jlb_solver *s, uint8_t *phase) {
     }
 }
 
+// extents (na, nb) of the face arrays of face `face`: x faces (NJ, NK), y
+// faces (NI, NK), z faces (NI, NJ) (jyulb/isothermal.pyx:253-265)
+void face_extent(const jlb_solver *s, int face, int &na, int &nb) {
+    const int ax = face >> 1;
+    na = ax == 0 ? s->NJ : s->NI;
+    nb = ax == 2 ? s->NJ : s->NK;
+}
+
+// faces whose bc data the reference refreshes at every evolve call: the
+// fixed faces, with Z1 refreshed when bc[Z1] is FIXED_DEN or bc[1Z] is
+// FIXED_VEL (jyulb/isothermal.pyx:476-502, the condition at :500)
+bool bc_refreshed(const jlb_solver *s, int face) {
+    const int *bc = s->cfg.bc;
+    return face == 5 ? (bc[5] == BC_FIXED_DEN || bc[4] == BC_FIXED_VEL) : is_fixed(bc[face]);
+}
+
+// Solver._set_bc_data (jyulb/isothermal.pyx:476-502): copies the whole first
+// or last interior layer of den / vel (halo rows included) for every
+// refreshed face; called at the start of evolve, before the halo rules
+void snapshot_bc_data(jlb_solver *s, const double *den, const double *vel) {
+    for (int face = 0; face < 6; ++face) {
+        if (!bc_refreshed(s, face)) continue;
+        const int ax = face >> 1;
+        const int layer = (face & 1) ? (ax == 0 ? s->NI : ax == 1 ? s->NJ : s->NK) - 2 : 1;
+        int na, nb;
+        face_extent(s, face, na, nb);
+        std::vector<double> &bd = s->bcd_den[face], &bv = s->bcd_vel[face];
+        bd.resize((size_t)na * nb);
+        bv.resize((size_t)3 * na * nb);
+#pragma omp parallel for schedule(static) if ((int64_t)na * nb > 65536)
+        for (int a = 0; a < na; ++a) {
+            for (int b = 0; b < nb; ++b) {
+                int I, J, K;
+                plane(ax, layer, a, b, I, J, K);
+                const int64_t n = fidx(s, I, J, K);
+                const size_t o = (size_t)a * nb + b;
+                bd[o] = den[n];
+                bv[3 * o] = vel[3 * n];
+                bv[3 * o + 1] = vel[3 * n + 1];
+                bv[3 * o + 2] = vel[3 * n + 2];
+            }
+        }
+    }
+}
+
 // jyulb/isothermal.pyx:582-686
 void enforce_den_vel(const jlb_solver *s, double *den, double *vel) {
     for (int face = 0; face < 6; ++face) {
@@ -934,6 +979,25 @@ int download(jlb_solver *s, double *den, double *vel) {
     return r;
 }
 
+// Halo rules of den / vel (enforce_den_vel) applied to the moments of the
+// last moment-writing step: the fluid sites of the layers they read are
+// written into the host arrays first (in place for page-locked arrays, else
+// by a full download)
+int halo_from_moments(jlb_solver *s, double *den, double *vel, unsigned axes) {
+    double *dd = (double *)dev_view(den), *dv = (double *)dev_view(vel);
+    if (dd && dv) {
+        CKR(aux_download_layers(s->prec, s->geom, axes, s->nmask, s->mom[0], s->mom[1], s->mom[2], s->mom[3], dd, dv,
+                                s->st));
+        ++s->launches;
+        CK(cudaStreamSynchronize(s->st));
+    } else {
+        int r = download(s, den, vel);
+        if (r) return r;
+    }
+    enforce_den_vel(s, den, vel);
+    return JLB_OK;
+}
+
 // The last step of an evolve call with its download overlapped: the
 // boundary nodes first, then the dense sweep in slabs of i-planes, each slab
 // followed by its FP64 assembly and (on a second stream) its pitched copy to
@@ -1273,10 +1337,13 @@ int jlb_set_static_halo(jlb_solver *s, int on) {
 int jlb_evolve(jlb_solver *s, uint32_t tsteps, const double g[3], double *den, double *vel, const double *acc,
                uint32_t *tot) {
     if (!s) return fail(s, JLB_ERR_INVALID_ARG, "NULL solver");
+    if (!den || !vel) return fail(s, JLB_ERR_INVALID_ARG, "NULL den/vel");
+    // the reference copies the bc data first, before its own checks and halo
+    // rules (jyulb/isothermal.pyx:1398)
+    snapshot_bc_data(s, den, vel);
     if (!s->init_done)
         return fail(s, JLB_ERR_STATE, "Finalize solver initialization before calling evolve\n"
                                       "(i.e. call first the method finalize_init)!");
-    if (!den || !vel) return fail(s, JLB_ERR_INVALID_ARG, "NULL den/vel");
     if (g) {
         for (int d = 0; d < 3; ++d) {
             if (!std::isfinite(g[d])) return fail(s, JLB_ERR_INVALID_ARG, "Invalid gravity input.");
@@ -1324,7 +1391,22 @@ int jlb_evolve(jlb_solver *s, uint32_t tsteps, const double g[3], double *den, d
     if (s->cfg.kernel == JLB_KERNEL_CXX && s->M > 0)
         return fail(s, JLB_ERR_UNSUPPORTED, "the C++-executable kernel has no moving solids");
     const bool overlap = !overlap_off() && !s->sparse && dma_ready(s, den, vel);
-    r = run_steps(s, overlap ? tsteps - 1 : tsteps, !overlap);
+    // The reference refreshes the periodic / symmetric halos of den and vel
+    // at the start of every step (jyulb/isothermal.pyx:1408-1411), so after
+    // evolve(n) they hold the images of step n-1's moments: run n-1 steps with
+    // moments, bring the layers the halo rules read into the host arrays,
+    // apply the rules, then the last step (whose download rewrites the fluid
+    // sites of those layers)
+    unsigned halo_axes = 0;
+    for (int face = 0; face < 6; ++face)
+        if (s->cfg.bc[face] == BC_PERIODIC || s->cfg.bc[face] == BC_SYMMETRIC) halo_axes |= 1u << (face >> 1);
+    uint32_t remaining = tsteps;
+    if (halo_axes && tsteps >= 2) {
+        if ((r = run_steps(s, tsteps - 1, true))) return r;
+        if ((r = halo_from_moments(s, den, vel, halo_axes))) return r;
+        remaining = 1;
+    }
+    r = run_steps(s, overlap ? remaining - 1 : remaining, !overlap);
     if (r) return r;
     s->host_t[3] += since(t1);
     t1 = clk::now();
@@ -1449,6 +1531,23 @@ int jlb_flow_info(jlb_solver *s, double ref_den, double out[12]) {
     out[9] = v[11];
     out[10] = v[9];
     out[11] = v[10];
+    return JLB_OK;
+}
+
+int jlb_bc_data(const jlb_solver *s, int32_t face, double *den, double *vel) {
+    if (!s || face < 0 || face > 5) return JLB_ERR_INVALID_ARG;
+    int na, nb;
+    face_extent(s, face, na, nb);
+    const size_t n = (size_t)na * nb;
+    const std::vector<double> &bd = s->bcd_den[face], &bv = s->bcd_vel[face];
+    if (den) {
+        if (bd.size() == n) std::memcpy(den, bd.data(), n * sizeof(double));
+        else std::fill(den, den + n, 1.0);
+    }
+    if (vel) {
+        if (bv.size() == 3 * n) std::memcpy(vel, bv.data(), 3 * n * sizeof(double));
+        else std::fill(vel, vel + 3 * n, 0.0);
+    }
     return JLB_OK;
 }
 

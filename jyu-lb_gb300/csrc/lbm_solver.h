@@ -64,6 +64,10 @@ struct jlb_solver {
     std::vector<uint8_t> hcls;       // Np node classes derived from hmask
     std::vector<int64_t> wall_pos;   // solid positions next to fluid (halo-padded index)
     std::vector<double> wall_vel;    // their velocities at the last classification
+    // the reference's bc_data_den_face_* / bc_data_vel_face_* arrays: the
+    // face layers of den / vel as the last evolve call read them (empty:
+    // never refreshed, den = 1 and vel = 0)
+    std::vector<double> bcd_den[6], bcd_vel[6];
     std::vector<int64_t> wall_chk;   // indices into wall_pos re-read at every evolve call
     bool static_halo = false;        // halo cells of closed faces are not written by the caller
     int64_t *d_wall_pos = nullptr;   // device copies of the checked wall_pos / wall_vel

@@ -23,7 +23,7 @@ JLB_ERR_NUMERIC = -6
 # every symbol include/jyulb_gb300.h declares
 EXPORTED_SYMBOLS = (
     "jlb_check_config", "jlb_create", "jlb_destroy", "jlb_finalize_init", "jlb_set_acc", "jlb_set_static_halo", "jlb_evolve",
-    "jlb_step", "jlb_download_moments", "jlb_get_populations", "jlb_set_populations",
+    "jlb_step", "jlb_download_moments", "jlb_get_populations", "jlb_set_populations", "jlb_bc_data",
     "jlb_reduce", "jlb_residual", "jlb_flow_info", "jlb_reduce_moments_noalloc", "jlb_tot_tsteps", "jlb_rlx_prm", "jlb_kernel_launches",
     "jlb_transfer_bytes", "jlb_host_timers",
     "jlb_last_error", "jlb_batch_create", "jlb_batch_destroy", "jlb_batch_step", "jlb_batch_moments",
@@ -98,6 +98,7 @@ def load() -> ctypes.CDLL:
         "jlb_download_moments": (ctypes.c_int, [vp, dp, dp]),
         "jlb_get_populations": (ctypes.c_int, [vp, dp]),
         "jlb_set_populations": (ctypes.c_int, [vp, dp]),
+        "jlb_bc_data": (ctypes.c_int, [vp, ctypes.c_int32, dp, dp]),
         "jlb_reduce": (ctypes.c_int, [vp, dp]),
         "jlb_residual": (ctypes.c_int, [vp, dp]),
         "jlb_flow_info": (ctypes.c_int, [vp, ctypes.c_double, dp]),

@@ -304,14 +304,13 @@ class Solver:
         (jyulb/isothermal.pyx:1370-1418)."""
         if self.error_occured():
             raise RuntimeError('Invalid solver setup: evolve aborted!')
-        if self.init_done == 0:
-            raise RuntimeError('Finalize solver initialization before calling evolve\n'
-                               '(i.e. call first the method finalize_init)!')
-        if self.fluid_lsite_domain is None:
-            return self.tot_tsteps
         acc = _native.dptr(self._acc) if self._acc_exposed else None
         tsteps = int(tsteps)
-        if not (self._keep_f2 and tsteps > 0):
+        # the engine copies the bc data first, as the reference does before
+        # its own checks (jyulb/isothermal.pyx:1398), then raises the
+        # reference's RuntimeError if finalize_init has not been called, and
+        # returns the step count unchanged on a lattice without fluid sites
+        if self.init_done == 0 or self.fluid_lsite_domain is None or not (self._keep_f2 and tsteps > 0):
             self.tot_tsteps = self._jlb_evolve(tsteps, acc)
             return self.tot_tsteps
         if tsteps == 1:
@@ -321,6 +320,9 @@ class Solver:
             # n-1 steps, a copy of the populations, then the last step on the
             # device with the inputs this call read, as inside one evolve(n)
             self._jlb_evolve(tsteps - 1, acc)
+            # the last step's halo rules read step n-1's moments, which the
+            # host arrays now hold (jyulb/isothermal.pyx:1408-1411)
+            self._enforce_den_vel_per_sym_bc()
             prev = self.populations()
             rc = self._lib.jlb_step(self._h, 1, 1)
             if rc == _native.JLB_OK:
@@ -330,6 +332,33 @@ class Solver:
             self.tot_tsteps = int(self._lib.jlb_tot_tsteps(self._h))
         self._f2 = prev
         return self.tot_tsteps
+
+    def _enforce_den_vel_per_sym_bc(self):
+        """Periodic copy / symmetric mirror of den and vel into the halo layers
+        of the host arrays, face by face in the reference's order and index
+        coverage (jyulb/isothermal.pyx:582-686): x faces cover the interior
+        (j, k), y faces all i and interior k, z faces all (i, j); a symmetric
+        face flips the normal velocity component."""
+        for face in range(6):
+            b = self._bc[face]
+            if b not in (PERIODIC, SYMMETRIC):
+                continue
+            ax, side = face // 2, face % 2
+            n = (self.NI, self.NJ, self.NK)[ax]
+            per = b == PERIODIC
+            rd, wr = (1, n - 1 if per else 0) if side == 0 else (n - 2, 0 if per else n - 1)
+            inner_j, inner_k = slice(1, self.NJ - 1), slice(1, self.NK - 1)
+            if ax == 0:
+                r, w = (rd, inner_j, inner_k), (wr, inner_j, inner_k)
+            elif ax == 1:
+                r, w = (slice(None), rd, inner_k), (slice(None), wr, inner_k)
+            else:
+                r, w = (slice(None), slice(None), rd), (slice(None), slice(None), wr)
+            self.den[w] = self.den[r]
+            v = self.vel[r].copy()
+            if not per:
+                v[..., ax] = -v[..., ax]
+            self.vel[w] = v
 
     def _jlb_evolve(self, tsteps, acc):
         tot = ctypes.c_uint32()
@@ -443,6 +472,21 @@ class Solver:
             self._raise(rc)
         return dict(zip(self.FLOW_INFO_KEYS, (float(v) for v in out)))
 
+    # bc_data_den_face_* / bc_data_vel_face_* (jyulb/isothermal.pxd:159-171):
+    # the face layers of den and vel that the last evolve call read
+    def _bc_data(self, face):
+        ax = face // 2
+        na = self.NJ if ax == 0 else self.NI
+        nb = self.NJ if ax == 2 else self.NK
+        den = np.empty((na, nb))
+        vel = np.empty((na, nb, 3))
+        rc = self._lib.jlb_bc_data(self._h, face, _native.dptr(den), _native.dptr(vel))
+        if rc != _native.JLB_OK:
+            self._raise(rc)
+        den.flags.writeable = False
+        vel.flags.writeable = False
+        return den, vel
+
     @property
     def kernel_launches(self):
         return int(self._lib.jlb_kernel_launches(self._h))
@@ -457,3 +501,19 @@ class Solver:
     def _need_init(self):
         if not self.init_done:
             raise RuntimeError('finalize_init has not been called')
+
+
+def _bc_data_property(face, which):
+    def get(self):
+        return self._bc_data(face)[which]
+    name = ("den", "vel")[which]
+    get.__doc__ = (f"Readonly copy of the {name} face layer of face {_FACE_NAMES[face]} read by the last "
+                   "evolve call (den = 1, vel = 0 before the first and on faces the reference does not refresh).")
+    return property(get)
+
+
+_FACE_NAMES = ("1X", "X1", "1Y", "Y1", "1Z", "Z1")
+for _face, _name in enumerate(_FACE_NAMES):
+    setattr(Solver, f"bc_data_den_face_{_name}", _bc_data_property(_face, 0))
+    setattr(Solver, f"bc_data_vel_face_{_name}", _bc_data_property(_face, 1))
+del _face, _name

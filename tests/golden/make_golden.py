@@ -5,8 +5,11 @@ oracle/_ref by oracle/build_ref.py) on small seeded cases.
 Each fixture stores the case description, the exact inputs (interior phase,
 den, vel, acc), the evolve-call chunking, and the reference's outputs after the
 last call: post-collision populations decoded from Solver.f1's Bundle-C layout
-(jyulb/isothermal.pyx:1532-1704) into (19, nx, ny, nz), and the interior den
-and vel.  Run from the repository root:
+(jyulb/isothermal.pyx:1532-1704) into (19, nx, ny, nz), the interior den
+and vel, the full halo-padded den and vel arrays (den_full, vel_full), and
+the twelve readonly bc-data face arrays
+(bc_data_den_face_* / bc_data_vel_face_*, jyulb/isothermal.pxd:159-171) as
+bcd_den_<face> / bcd_vel_<face>.  Run from the repository root:
 
     python oracle/build_ref.py && python tests/golden/make_golden.py [case ...]
 """
@@ -25,6 +28,7 @@ sys.path.insert(0, os.path.join(ROOT, "oracle", "_ref"))
 from jyulb.isothermal import Solver  # noqa: E402  (the reference build)
 
 BGK, TRT, REG = 0, 1, 2
+FACES = ("1X", "X1", "1Y", "Y1", "1Z", "Z1")
 WALL, PER, FD, FV, SYM = 0, 1, 2, 3, 4
 
 
@@ -162,20 +166,24 @@ def run(case):
     nf = s.finalize_init()
     for c in case["chunks"]:
         s.evolve(c)
-    return nf, decode_bundle_c(s), np.array(s.get_den()), np.array(s.get_vel())
+    bcd = {"den_full": np.array(s.den), "vel_full": np.array(s.vel)}
+    for face in FACES:
+        bcd["bcd_den_" + face] = np.array(getattr(s, "bc_data_den_face_" + face))
+        bcd["bcd_vel_" + face] = np.array(getattr(s, "bc_data_vel_face_" + face))
+    return nf, decode_bundle_c(s), np.array(s.get_den()), np.array(s.get_vel()), bcd
 
 
 def main(names=None):
     for case in cases():
         if names and case["name"] not in names:
             continue
-        nf, f, den, vel = run(case)
+        nf, f, den, vel, bcd = run(case)
         meta = {k: case[k] for k in ("name", "lat", "scheme", "kvisc", "g", "bc", "chunks")}
         meta["nfluid"] = int(nf)
         path = os.path.join(HERE, case["name"] + ".npz")
         acc = case["acc"] if case["acc"] is not None else np.zeros(0)
         np.savez_compressed(path, meta=json.dumps(meta), phase=case["phase"], den0=case["den"],
-                            vel0=case["vel"], acc0=acc, f=f, den=den, vel=vel)
+                            vel0=case["vel"], acc0=acc, f=f, den=den, vel=vel, **bcd)
         print(f"{case['name']:18s} fluid={nf:5d} -> {os.path.relpath(path, ROOT)} "
               f"({os.path.getsize(path) // 1024} KB)")
 

@@ -19,6 +19,11 @@ def load_case(name):
     c.update(phase=z["phase"], den0=z["den0"], vel0=z["vel0"],
              acc0=z["acc0"] if z["acc0"].size else None,
              f=z["f"], den=z["den"], vel=z["vel"])
+    # the reference's full halo-padded den / vel and its twelve bc-data face
+    # arrays after the last evolve call
+    for k in z.files:
+        if k in ("den_full", "vel_full") or k.startswith("bcd_"):
+            c[k] = z[k]
     return c
 
 
