@@ -68,7 +68,10 @@ def test_fp64_adjoint_matches_torch_autograd(scheme, zb_name):
 
 
 @pytest.mark.parametrize("scheme", [1, 2])
-@pytest.mark.parametrize("precision,tol", [(0, 1e-6), (1, 2e-3)])
+# FP32: the adjoint of the FP32 model against differences of the FP64 model,
+# so the bound covers both the adjoint and the FP32 model's rounding (measured
+# <= 1e-6 here, 4e-5 on a 40x16x8 channel over 300 steps)
+@pytest.mark.parametrize("precision,tol", [(0, 1e-6), (1, 1e-4)])
 def test_adjoint_matches_central_differences(precision, tol, scheme):
     from jyulb.adjoint import ChannelProblem
     from jyulb.defs import FP64
