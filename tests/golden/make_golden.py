@@ -155,6 +155,42 @@ def cases():
     return out
 
 
+def large_cases():
+    """1000-step cases on lattices where the engine's size-dependent paths run
+    (consecutive-site blocks for nz not a multiple of 32; whole 128-site rows
+    for the bulk-copy staged step; boundary-node tables over many blocks).
+    Their arrays are stored as SHA-256 digests of the float64 bytes (C
+    order, little endian; f, den and vel over the fluid sites only) plus a
+    strided sample, not in full."""
+    out = []
+    # TRT cavity with the reference's fixed magic 3/16, Zou-He lid on Y1,
+    # nz = 42
+    sh = (40, 48, 42)
+    ph = np.ones(sh, np.uint8)
+    vel = np.zeros(sh + (3,)); vel[:, -1, :, 0] = 0.05
+    out.append(dict(name="large_cavity_trt", lat=list(sh), scheme=TRT, kvisc=0.02, g=[0, 0, 0],
+                    bc=[WALL, WALL, WALL, FV, WALL, WALL], phase=ph, den=np.ones(sh), vel=vel, acc=None,
+                    chunks=[1000]))
+    # regularized channel through seeded spheres (90% fluid), gravity along
+    # x, periodic x/z, wall below and symmetric face on top, nz = 128
+    rng = np.random.default_rng(31)
+    sh = (64, 32, 128)
+    ph = spheres(sh, 4.0, 0.9, rng)
+    out.append(dict(name="large_channel_reg", lat=list(sh), scheme=REG, kvisc=(0.7 - 0.5) / 3.0,
+                    g=[5e-6, 0, 0], bc=[PER, PER, WALL, SYM, PER, PER], phase=ph, den=np.ones(sh),
+                    vel=np.zeros(sh + (3,)), acc=None, chunks=[600, 400]))
+    return out
+
+
+def digest(a) -> str:
+    import hashlib
+
+    return hashlib.sha256(np.ascontiguousarray(a, dtype="<f8").tobytes()).hexdigest()
+
+
+SAMPLE_STRIDE = 97  # every 97th value of the flattened arrays goes into the sample
+
+
 def run(case):
     s = Solver(np.array(case["lat"], dtype=np.int32), case["scheme"], case["kvisc"],
                np.array(case["g"], dtype=np.float64), np.array(case["bc"], dtype=np.int32))
@@ -174,7 +210,7 @@ def run(case):
 
 
 def main(names=None):
-    for case in cases():
+    for case in cases() + large_cases():
         if names and case["name"] not in names:
             continue
         nf, f, den, vel, bcd = run(case)
@@ -182,8 +218,18 @@ def main(names=None):
         meta["nfluid"] = int(nf)
         path = os.path.join(HERE, case["name"] + ".npz")
         acc = case["acc"] if case["acc"] is not None else np.zeros(0)
+        arrays = dict(f=f, den=den, vel=vel, **bcd)
+        if case["name"].startswith("large_"):
+            # f, den and vel over the fluid sites (what the solver defines),
+            # the halo-padded arrays and bc data whole
+            fl = case["phase"] != 0
+            arrays.update(f=f[:, fl], den=den[fl], vel=vel[fl])
+            meta["sha256"] = {k: digest(a) for k, a in arrays.items()}
+            meta["sample_stride"] = SAMPLE_STRIDE
+            arrays = {k + "_sample": np.ascontiguousarray(a).reshape(-1)[::SAMPLE_STRIDE]
+                      for k, a in (("f", f), ("den", den), ("vel", vel))}
         np.savez_compressed(path, meta=json.dumps(meta), phase=case["phase"], den0=case["den"],
-                            vel0=case["vel"], acc0=acc, f=f, den=den, vel=vel, **bcd)
+                            vel0=case["vel"], acc0=acc, **arrays)
         print(f"{case['name']:18s} fluid={nf:5d} -> {os.path.relpath(path, ROOT)} "
               f"({os.path.getsize(path) // 1024} KB)")
 

@@ -5,7 +5,7 @@ match is exact."""
 import numpy as np
 import pytest
 
-from helpers import CASES, load_case, run_oracle
+from helpers import CASES, LARGE_CASES, digest, load_case, run_oracle
 
 
 @pytest.mark.parametrize("name", CASES)
@@ -110,3 +110,26 @@ def test_oracle_halo_arrays_match_reference_bitwise(name):
         o.evolve(n)
     np.testing.assert_array_equal(o.den, c["den_full"])
     np.testing.assert_array_equal(o.vel, c["vel_full"])
+
+
+@pytest.mark.parametrize("name", LARGE_CASES)
+def test_oracle_matches_reference_digests_at_1000_steps(name):
+    # the 1000-step fixtures on larger lattices: SHA-256 digests of the
+    # reference's float64 arrays
+    from pyoracle import Oracle
+
+    c = load_case(name)
+    o = Oracle(c["lat"], c["scheme"], c["kvisc"], c["g"], c["bc"], 0.0)
+    o.get_phase()[:] = c["phase"]
+    o.get_den()[:] = c["den0"]
+    o.get_vel()[:] = c["vel0"]
+    assert o.finalize_init() == c["nfluid"]
+    for n in c["chunks"]:
+        o.evolve(n)
+    fl = c["phase"] != 0
+    h = c["sha256"]
+    assert digest(o.populations()[:, fl]) == h["f"]
+    assert digest(o.get_den()[fl]) == h["den"]
+    assert digest(o.get_vel()[fl]) == h["vel"]
+    assert digest(o.den) == h["den_full"]
+    assert digest(o.vel) == h["vel_full"]
