@@ -600,31 +600,25 @@ def adjoint_block(args):
     big = np.unravel_index(np.argsort(np.abs(duin).ravel())[-2:], duin.shape)
     checks = []
 
-    def loss32(tau, g, uin):
-        return p32.forward(tau, g, uin, steps, target)[0]
-
-    def fd(name, h, h32, plus, minus, adj32, adj64):
-        # central differences of the FP64 model (step h) and of the FP32 model
-        # itself (a larger step h32 over its rounding); a parameter whose
-        # influence has not reached the loss plane yet has d = 0
+    def fd(name, h, plus, minus, adj32, adj64):
+        # central differences of the FP64 model; a parameter whose influence
+        # has not reached the loss plane yet has d = 0
         d = (loss64(*plus(h)) - loss64(*minus(h))) / (2 * h)
-        d32 = (loss32(*plus(h32)) - loss32(*minus(h32))) / (2 * h32)
-        checks.append({"param": name, "fd_fp64": d, "fd_fp32": d32, "adjoint_fp32": adj32, "adjoint_fp64": adj64,
+        checks.append({"param": name, "fd_fp64": d, "adjoint_fp32": adj32, "adjoint_fp64": adj64,
                        "rel_err_fp32": abs(adj32 - d) / abs(d) if d else None,
                        "rel_err_fp64": abs(adj64 - d) / abs(d) if d else None,
-                       "rel_err_fp32_vs_fd_fp32": abs(adj32 - d32) / abs(d32) if d32 else None,
                        "rel_diff_fp32_vs_fp64_adjoint": abs(adj32 - adj64) / abs(adj64) if adj64 else None})
 
     ex = np.array([1.0, 0.0, 0.0])
-    fd("tau", 1e-4, 1e-3, lambda h: (tau0 + h, g0, uin0), lambda h: (tau0 - h, g0, uin0), dtau, a64[0])
-    fd("gx", 1e-9, 1e-8, lambda h: (tau0, g0 + h * ex, uin0), lambda h: (tau0, g0 - h * ex, uin0), dg[0],
+    fd("tau", 1e-4, lambda h: (tau0 + h, g0, uin0), lambda h: (tau0 - h, g0, uin0), dtau, a64[0])
+    fd("gx", 1e-9, lambda h: (tau0, g0 + h * ex, uin0), lambda h: (tau0, g0 - h * ex, uin0), dg[0],
        a64[1][0])
-    fd("uin.v (random +-1 direction over the inlet)", 1e-6, 1e-5, lambda h: (tau0, g0, uin0 + h * v),
+    fd("uin.v (random +-1 direction over the inlet)", 1e-6, lambda h: (tau0, g0, uin0 + h * v),
        lambda h: (tau0, g0, uin0 - h * v), float((duin * v).sum()), float((a64[2] * v).sum()))
     for j, k in zip(*big):
         du = np.zeros_like(uin0)
         du[j, k] = 1.0
-        fd(f"uin[{j},{k}]", 1e-6, 1e-4, lambda h: (tau0, g0, uin0 + h * du), lambda h: (tau0, g0, uin0 - h * du),
+        fd(f"uin[{j},{k}]", 1e-6, lambda h: (tau0, g0, uin0 + h * du), lambda h: (tau0, g0, uin0 - h * du),
            float(duin[j, k]), float(a64[2][j, k]))
     peak, peak_kind = measured_peak()
     rev_ms = med["reverse"] / steps
@@ -660,11 +654,11 @@ def adjoint_block(args):
                                       default=None),
         "max_rel_err_fp64_vs_fd": max((c["rel_err_fp64"] for c in checks if c["rel_err_fp64"] is not None),
                                       default=None),
-        "max_rel_err_fp32_vs_fd_fp32": max((c["rel_err_fp32_vs_fd_fp32"] for c in checks
-                                            if c["rel_err_fp32_vs_fd_fp32"] is not None), default=None),
         "gradient_note": "rel_err_fp32 compares the FP32 adjoint with differences of the FP64 model, so it "
-                         "includes the FP32 model's own rounding; rel_err_fp32_vs_fd_fp32 differences the FP32 "
-                         "model itself",
+                         "includes the FP32 model's own rounding (its loss differs from the FP64 model's by "
+                         "the relative amount in loss_rel_diff); rel_diff_fp32_vs_fp64_adjoint is that gap "
+                         "between the two adjoints",
+        "loss_rel_diff": abs(L - L64) / abs(L64),
         "e2e": {"value": round(statistics.median(walls) * 1e3, 2), "unit": "ms per forward+backward through "
                 "jyulb.adjoint (host parameters in, gradients out)",
                 "h2d_bytes_per_step": int(8 * (uin0.size + target.size + 4)),
