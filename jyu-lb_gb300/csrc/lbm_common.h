@@ -111,6 +111,8 @@ struct StepArgs {
     int bx, by, kblocks;  // block shape and k-blocks per row-block
     int nb_dense;         // number of dense blocks; the rest are boundary blocks
     int b0;               // first dense block of this launch (a launch may cover a slab)
+    int pf;               // L2 prefetch distance in dense blocks (0: none): block b
+                          // prefetches the rows block b + pf will read
     // linear mapping, used when nz is not a multiple of 32 (a warp along k
     // alone would leave lanes idle): dense block b takes the sites
     // [128 b, 128 b + 128) of n = (i*ny + j)*nz + k, with blocks of (128, 1)

@@ -626,6 +626,7 @@ StepArgs make_args(const jlb_solver *s, int write_moments) {
         a.div_nz = make_udiv((uint32_t)s->nz);
         a.nb_dense = (int)((s->N + 127) / 128);
     }
+    a.pf = s->pf_blocks;
     a.M = s->M;
     a.sp_node = s->d_sp_node; a.sp_info = s->d_sp_info;
     a.sp_rd = s->d_sp_rd; a.sp_wr = s->d_sp_wr;
@@ -684,6 +685,22 @@ int launch_one(jlb_solver *s, const StepArgs &a, bool pstep) {
 // staging, JLB_TMA=1 stages both steps.
 void choose_kernel(jlb_solver *s) {
     s->use_tma = false;
+    // L2 line prefetch 6 blocks per SM ahead (of the 8 resident) on the
+    // direct FP32 kernels: 38.8 -> 39.8 GLUPS on the 256^3 cavity, flat from
+    // 5 to 8 blocks per SM, worse beyond.  FP16 storage is issue-bound and
+    // loses (50.8 -> 48.5), FP64 is bound by its arithmetic.  JLB_PF=<blocks>
+    // sets the distance for any precision, 0 switches it off
+    {
+        int dev = 0, sms = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+            cudaGetLastError();
+            sms = 0;
+        }
+        const char *ep = std::getenv("JLB_PF");
+        s->pf_blocks = (ep && ep[0]) ? std::max(0, std::atoi(ep)) : (s->prec == PREC_FP32 ? 6 * sms : 0);
+        ++s->args_version;
+    }
     // fluid-only layout for FP32 / FP16 storage when under 80% of the sites
     // are fluid: a lattice-ordered sweep then fetches population lines that
     // are partly solid slots (1.6x the fluid bytes at porosity 0.6).

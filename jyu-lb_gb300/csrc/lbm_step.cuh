@@ -440,6 +440,51 @@ __device__ __forceinline__ void sparse_node(const StepArgs &a, int b) {
     }
 }
 
+// ---------------------------------------------------------------------------
+// L2 prefetch of a dense block's source rows.  The direct kernels hold their
+// 19 loads per site in registers, which caps the loads in flight per SM; line
+// prefetches into L2 (one warp, no registers held) issued one resident wave
+// ahead let the later loads hit L2.  Block b covers one contiguous run
+// of sites [n0, n0 + cnt) under both mappings; the P step reads slot opp(q)
+// at n - c_q (wraps aside), the L step slot q at n.  Ranges are clamped to
+// the slot's sites and widened to 16-byte boundaries.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void prefetch_line(const void *p) {
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+
+// called by all 32 lanes of one warp: lane l prefetches lines l, l + 32, ...
+// of the block's 19 source rows
+template <class S, bool PSTEP>
+__device__ __forceinline__ void prefetch_block(const StepArgs &a, int b, int lane) {
+    int64_t n0, cnt;
+    const int64_t N = (int64_t)a.nx * a.ny * a.nz;
+    if (a.lin) {
+        n0 = (int64_t)b * 128;
+        cnt = 128;
+    } else {
+        const int kb = b % a.kblocks, rb = b / a.kblocks;
+        const int k0 = kb * a.bx;
+        n0 = (int64_t)rb * a.by * a.nz + k0;
+        cnt = a.kblocks == 1 ? (int64_t)a.by * a.nz : (int64_t)min(a.bx, a.nz - k0);
+    }
+    if (n0 >= N) return;
+    if (n0 + cnt > N) cnt = N - n0;
+    const char *f = (const char *)a.f;
+    const int64_t syz = (int64_t)a.ny * a.nz;
+    constexpr int LPR = 128 * (int)sizeof(S) / 128 + 1; // 128-byte lines per source row
+#pragma unroll 1
+    for (int idx = lane; idx < Q * LPR; idx += 32) {
+        const int q = idx / LPR, line = idx - q * LPR;
+        const int64_t d = PSTEP ? (int64_t)CX(q) * syz + (int64_t)CY(q) * a.nz + CZ(q) : 0;
+        int64_t e = n0 - d - 1 + (int64_t)line * (128 / (int)sizeof(S));
+        if (e < 0) e = 0;
+        if (e >= N) continue;
+        const int slot = PSTEP ? OPP(q) : q;
+        prefetch_line(f + (slot * a.Np + e) * (int64_t)sizeof(S));
+    }
+}
+
 // resident 128-thread blocks per SM asked of the register allocator, per
 // kernel kind (the build sets them per storage type)
 #ifndef JLB_MIN_BLOCKS
@@ -460,8 +505,13 @@ __device__ __forceinline__ void sparse_node(const StepArgs &a, int b) {
 template <class ST, class PH, bool PSTEP, bool ACCF, class IT>
 __global__ void __launch_bounds__(128, JLB_MIN_BLOCKS_STEP) lbm_step_kernel(const StepArgs a) {
     const int b = (int)blockIdx.x;
-    if (b < a.nb_dense) dense_node<ST, PH, PSTEP, ACCF, IT>(a, b + a.b0);
-    else special_node<ST, PH, PSTEP, ACCF>(a, b - a.nb_dense);
+    if (b < a.nb_dense) {
+        if (a.pf && threadIdx.y == 0 && threadIdx.x < 32 && b + a.pf < a.nb_dense)
+            prefetch_block<typename ST::S, PSTEP>(a, b + a.pf + a.b0, (int)threadIdx.x);
+        dense_node<ST, PH, PSTEP, ACCF, IT>(a, b + a.b0);
+    } else {
+        special_node<ST, PH, PSTEP, ACCF>(a, b - a.nb_dense);
+    }
 }
 
 template <class ST, class PH, bool PSTEP, bool ACCF>
