@@ -60,6 +60,9 @@ extern "C" {
 #define JLB_FP64 0 /* FP64 storage and arithmetic (parity path)          */
 #define JLB_FP32 1 /* FP32 storage of f_i - w_i, FP32 arithmetic          */
 #define JLB_FP16 2 /* FP16 storage of 2^12 (f_i/w_i - 1), FP32 arithmetic */
+#define JLB_FP64_FAST 3 /* FP64 storage and arithmetic, regrouped and FMA-
+                           contracted: within 1e-12 relative of JLB_FP64,
+                           not bit for bit (the reference has no such mode) */
 
 typedef struct jlb_solver jlb_solver;
 
@@ -69,7 +72,7 @@ typedef struct jlb_config {
     double kvisc;        /* kinematic viscosity, > 0                         */
     double g[3];         /* uniform gravity                                  */
     int32_t bc[6];       /* per face 1X,X1,1Y,Y1,1Z,Z1: JLB_WALL..SYMMETRIC  */
-    int32_t precision;   /* JLB_FP64 / JLB_FP32 / JLB_FP16                   */
+    int32_t precision;   /* JLB_FP64 / JLB_FP32 / JLB_FP16 / JLB_FP64_FAST   */
     double trt_magic;    /* TRT magic parameter; <= 0 selects the reference's
                             fixed 8(2-w)/(8-w) odd rate (magic 3/16)         */
     int32_t kernel;      /* JLB_KERNEL_JYULB (0) or JLB_KERNEL_CXX           */

@@ -24,6 +24,8 @@ COMMON = ["-std=c++20", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler",
 HOST_FLAGS = ["-x", "cu", "-Xcompiler", "-fopenmp", "-Xcompiler", "-ffp-contract=off"]
 UNITS = {
     "lbm_fp64.cu": ["-fmad=false"],
+    # the fast FP64 step: contracted on purpose
+    "lbm_fp64fast.cu": [],
     # resident 128-thread blocks per SM.  The direct steps are latency-bound
     # on HBM: 8 blocks (<= 64 registers, 32 warps) keep more loads in flight
     # than 6 or 7, even where a few registers spill.  The persistent staged L
@@ -45,7 +47,7 @@ UNITS = {
     "lbm_batch_host.cpp": HOST_FLAGS,
     "lbm_adjoint_host.cpp": HOST_FLAGS,
 }
-HEADERS = ["lbm_common.h", "lbm_solver.h", "lbm_step.cuh", "lbm_step_tma.cuh", "lbm_shifted.cuh", "lbm_aux.h", "lbm_batch.h", "lbm_adjoint.h"]
+HEADERS = ["lbm_common.h", "lbm_fp64.cuh", "lbm_solver.h", "lbm_step.cuh", "lbm_step_tma.cuh", "lbm_shifted.cuh", "lbm_aux.h", "lbm_batch.h", "lbm_adjoint.h"]
 
 
 def _nvcc() -> str:

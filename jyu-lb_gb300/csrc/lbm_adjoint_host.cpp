@@ -107,7 +107,8 @@ int jlb_adj_create(const jlb_config *cfg, const uint8_t *phase, int32_t loss_pla
     jlb_adjoint *A = nullptr;
     if (!cfg || !phase || !out) return afail(nullptr, JLB_ERR_INVALID_ARG, "NULL argument");
     *out = nullptr;
-    if (cfg->precision == JLB_FP16) return afail(nullptr, JLB_ERR_UNSUPPORTED, "adjoint supports FP64 and FP32");
+    if (cfg->precision != JLB_FP64 && cfg->precision != JLB_FP32)
+        return afail(nullptr, JLB_ERR_UNSUPPORTED, "adjoint supports FP64 and FP32");
     if (checkpoint_every < 1) return afail(nullptr, JLB_ERR_INVALID_ARG, "checkpoint interval must be >= 1");
     if (cfg->kernel != JLB_KERNEL_JYULB)
         return afail(nullptr, JLB_ERR_UNSUPPORTED, "adjoint supports the jyulb collision kernel");

@@ -149,6 +149,8 @@ constexpr int CXX_FORCE2 = 2;    // second-order forcing term instead of the fir
 // launch entry points, one per precision translation unit
 // grid: `blocks` blocks of (a.bx, a.by) threads; returns a cudaError_t value
 int launch_step_fp64(const StepArgs &a, int scheme, bool pstep, bool accf, int blocks, cudaStream_t st);
+// FP64 with contracted, regrouped arithmetic (lbm_fp64fast.cu)
+int launch_step_fp64fast(const StepArgs &a, int scheme, bool pstep, bool accf, int blocks, cudaStream_t st);
 int launch_step_fp32(const StepArgs &a, int scheme, bool pstep, bool accf, int blocks, cudaStream_t st);
 int launch_step_fp16(const StepArgs &a, int scheme, bool pstep, bool accf, int blocks, cudaStream_t st);
 // the same step on the fluid-only layout (a.csite/a.cidx set): blocks of 128

@@ -668,7 +668,10 @@ int launch_one(jlb_solver *s, const StepArgs &a, bool pstep) {
             r = launch_step_tma_fp16(a, s->cfg.rlx_scheme, pstep, s->accf, s->tma_grid, ntiles, nsb, s->d_err, s->st);
     } else if (s->cfg.kernel == JLB_KERNEL_CXX) {
         r = launch_step_cxx(a, s->cfg.rlx_scheme, s->cfg.kernel_opts, pstep, s->accf, blocks, s->st);
-    } else if (s->prec == PREC_FP64) r = launch_step_fp64(a, s->cfg.rlx_scheme, pstep, s->accf, blocks, s->st);
+    } else if (s->prec == PREC_FP64) {
+        r = s->fast64 ? launch_step_fp64fast(a, s->cfg.rlx_scheme, pstep, s->accf, blocks, s->st)
+                      : launch_step_fp64(a, s->cfg.rlx_scheme, pstep, s->accf, blocks, s->st);
+    }
     else if (s->prec == PREC_FP32) r = launch_step_fp32(a, s->cfg.rlx_scheme, pstep, s->accf, blocks, s->st);
     else r = launch_step_fp16(a, s->cfg.rlx_scheme, pstep, s->accf, blocks, s->st);
     if (r) return fail(s, JLB_ERR_CUDA, std::string("step launch: ") + cudaGetErrorString((cudaError_t)r));
@@ -1032,6 +1035,7 @@ int final_step_overlapped(jlb_solver *s, double *den, double *vel) {
     auto direct = [&](const StepArgs &x, int blocks) {
         int r;
         if (s->cfg.kernel == JLB_KERNEL_CXX) r = launch_step_cxx(x, s->cfg.rlx_scheme, s->cfg.kernel_opts, pstep, s->accf, blocks, s->st);
+        else if (s->prec == PREC_FP64 && s->fast64) r = launch_step_fp64fast(x, s->cfg.rlx_scheme, pstep, s->accf, blocks, s->st);
         else if (s->prec == PREC_FP64) r = launch_step_fp64(x, s->cfg.rlx_scheme, pstep, s->accf, blocks, s->st);
         else if (s->prec == PREC_FP32) r = launch_step_fp32(x, s->cfg.rlx_scheme, pstep, s->accf, blocks, s->st);
         else r = launch_step_fp16(x, s->cfg.rlx_scheme, pstep, s->accf, blocks, s->st);
@@ -1123,7 +1127,7 @@ int jlb_check_config(const jlb_config *cfg, char *msg, size_t msg_len) {
     for (int ax = 0; ax < 3; ++ax) fx[ax] = is_fixed(bc[2 * ax]) || is_fixed(bc[2 * ax + 1]);
     if ((fx[0] && (fx[1] || fx[2])) || (fx[1] && (fx[0] || fx[2])) || (fx[2] && (fx[0] || fx[1])))
         return bad("Invalid fixed variable bc setup.");
-    if (cfg->precision < JLB_FP64 || cfg->precision > JLB_FP16) return bad("Invalid precision input.");
+    if (cfg->precision < JLB_FP64 || cfg->precision > JLB_FP64_FAST) return bad("Invalid precision input.");
     if (std::isnan(cfg->trt_magic)) return bad("Invalid TRT magic parameter input.");
     for (int d = 0; d < 3; ++d)
         if (!std::isfinite(cfg->g[d])) return bad("Invalid gravity input.");
@@ -1160,7 +1164,10 @@ int jlb_create(const jlb_config *cfg, jlb_solver **out) {
     s->N = (int64_t)s->nx * s->ny * s->nz;
     s->Np = ((s->N + 127) / 128) * 128;
     s->NCNT = (int64_t)s->NI * s->NJ * s->NK;
-    s->prec = cfg->precision;
+    // JLB_FP64_FAST keeps the FP64 state and host paths; only the step
+    // kernel differs
+    s->fast64 = cfg->precision == JLB_FP64_FAST;
+    s->prec = s->fast64 ? PREC_FP64 : cfg->precision;
     s->ssz = s->prec == PREC_FP64 ? 8 : s->prec == PREC_FP32 ? 4 : 2;
     s->csz = s->prec == PREC_FP64 ? 8 : 4;
     for (int d = 0; d < 3; ++d) s->g[d] = cfg->g[d];

@@ -19,6 +19,7 @@ struct jlb_solver {
     int nx = 0, ny = 0, nz = 0, NI = 0, NJ = 0, NK = 0;
     int64_t N = 0, Np = 0, NCNT = 0;
     int prec = 0;
+    bool fast64 = false;  // JLB_FP64_FAST: FP64 state, the contracted step kernel
     size_t ssz = 8, csz = 8;  // storage / compute element sizes
     double we = 0, wo = 0;
     double tau = 0;       // relaxation time of the C++-executable model

@@ -67,3 +67,5 @@ SYMMETRIC = 4   # specular reflection
 FP64 = 0        # FP64 storage and arithmetic, the reference's operation order
 FP32 = 1        # FP32 storage of f - w, FP32 arithmetic
 FP16 = 2        # FP16 storage of 2^12 (f/w - 1), FP32 arithmetic
+FP64_FAST = 3   # FP64 storage and arithmetic, regrouped and FMA-contracted
+                # (within 1e-12 relative of FP64, not bit for bit)

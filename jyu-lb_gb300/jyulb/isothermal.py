@@ -24,7 +24,7 @@ writes them in place.  As in the reference:
   not reach, keep the values they had at ``finalize_init``.
 
 Additions of this engine (keyword-only): ``precision`` (defs.FP64 / FP32 /
-FP16), ``trt_magic`` (TRT magic parameter; None keeps the reference's 3/16) and
+FP16 / FP64_FAST), ``trt_magic`` (TRT magic parameter; None keeps the reference's 3/16) and
 ``stream`` (a cudaStream_t handle as int to run on; default: the engine's own),
 plus ``populations``, ``set_populations``, ``reduce``, ``save_state`` and
 ``load_state``.
@@ -38,7 +38,7 @@ import numpy as np
 from . import _native
 from .D3Q19 import D3Q19_H10, LVECS
 from .defs import (BGK, FACE_1X, FACE_1Y, FACE_1Z, FACE_X1, FACE_Y1, FACE_Z1, FIXED_DEN,
-                   FIXED_VEL, FP16, FP32, FP64, PERIODIC, REGULARIZATION, SOLID, SYMMETRIC,
+                   FIXED_VEL, FP16, FP32, FP64, FP64_FAST, PERIODIC, REGULARIZATION, SOLID, SYMMETRIC,
                    TRT, WALL, X, Y, Z)
 
 _ERRS = {
@@ -107,7 +107,7 @@ class Solver:
         if not kvisc > 0.0:
             self.error_msg = 'Invalid kinematic viscosity input.'
             raise ValueError(self.error_msg)
-        if precision not in (FP64, FP32, FP16):
+        if precision not in (FP64, FP32, FP16, FP64_FAST):
             raise ValueError('Invalid precision input.')
         self._g = np.zeros(3) if g is None else np.array([g[X], g[Y], g[Z]], dtype=np.float64)
         if bc is None:
