@@ -66,7 +66,7 @@ template <int SCH> struct Phys64F : Phys64FBase {
         C jx, jy, jz;
         C hx, hy, hz, hxx, hxy, hxz, hyy, hyz, hzz, H0;
         const C den = moments(f, jx, jy, jz);
-        const C inv = __drcp_rn(den); // = 1.0 / den, correctly rounded
+        const C inv = 1.0 / den;
         if (SCH == SCH_REG) {
             // H10 second moments of f (jyulb/D3Q19.pyx:395-452), relaxed
             // towards equilibrium; the projection drops the rest
