@@ -334,7 +334,13 @@ template <class C> __device__ __forceinline__ void block_sensitivities(C *pg, do
         if (lane == 0) sm[c][wid] = v;
     }
     __syncthreads();
-    if (tid < 5) slot[tid] += (double)sm[tid][0] + (double)sm[tid][1] + (double)sm[tid][2] + (double)sm[tid][3];
+    // blocks have 3 warps (96-site rows, nz = 96) or 4
+    const int nw = (int)(blockDim.x * blockDim.y + 31) >> 5;
+    if (tid < 5) {
+        double v = 0.0;
+        for (int w = 0; w < nw; ++w) v += (double)sm[tid][w];
+        slot[tid] += v;
+    }
 }
 
 // resident 128-thread blocks per SM asked of the register allocator (the
@@ -466,7 +472,7 @@ __device__ __forceinline__ void adjoint_boundary_sites(const AdjArgs &A, int b, 
     }
 }
 
-int adjoint_blocks(const StepArgs &a) { return a.nb_dense + (a.M + 127) / 128; }
+int adjoint_blocks(const StepArgs &a) { return a.nb_dense + special_blocks(a); }
 
 // One step of the reverse sweep: blocks [0, nb_dense) take the dense sites,
 // the rest the boundary sites (disjoint address sets, as in the forward step).

@@ -313,7 +313,7 @@ int jlb_adj_backward(jlb_adjoint *A, double *dtau, double dg[3], double *duin) {
             a.sp_tee = sp_in_of(seg, t);
             if (t + 1 == t1) a.nb_dense = 0;
             if (a.nb_dense == 0 && a.M == 0) continue;
-            const int blocks = a.nb_dense + (a.M + 127) / 128;
+            const int blocks = a.nb_dense + special_blocks(a);
             const bool pstep = (t & 1u) == 0;
             const int r = s->prec == PREC_FP64 ? launch_step_fp64(a, s->cfg.rlx_scheme, pstep, s->accf, blocks, st2)
                                                : launch_step_fp32(a, s->cfg.rlx_scheme, pstep, s->accf, blocks, st2);

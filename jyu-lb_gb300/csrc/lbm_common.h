@@ -142,6 +142,15 @@ struct StepArgs {
                           // boundary nodes, [19][M] in the storage type
 };
 
+// Blocks of the boundary-node path in a launch of the direct step kernel (or
+// the adjoint's reverse kernel), whose blocks have a.bx * a.by threads: 96
+// when nz = 96 (row blocks of one 96-site row), 128 otherwise.  The staged and
+// fluid-only kernels use 128-thread blocks.
+inline int special_blocks(const StepArgs &a) {
+    const int T = a.bx * a.by;
+    return (a.M + T - 1) / T;
+}
+
 // options of the C++-executable collision model (lbm_cxx.cu)
 constexpr int CXX_LINEAR_EQ = 1; // linear ("Stokes") equilibrium instead of the quadratic one
 constexpr int CXX_FORCE2 = 2;    // second-order forcing term instead of the first-order one

@@ -653,8 +653,8 @@ StepArgs make_args(const jlb_solver *s, int write_moments) {
 }
 
 int launch_one(jlb_solver *s, const StepArgs &a, bool pstep) {
-    const int blocks = a.nb_dense + (a.M + 127) / 128;
-    const int nsb = (a.M + 127) / 128;
+    const int blocks = a.nb_dense + special_blocks(a); // direct kernel: blocks of bx * by threads
+    const int nsb = (a.M + 127) / 128;                  // staged / fluid-only kernels: 128
     int r;
     if (a.csite) {
         const int nb = (int)((a.Nc + 127) / 128) + nsb;
@@ -1054,7 +1054,7 @@ int final_step_overlapped(jlb_solver *s, double *den, double *vel) {
     if (a.M > 0) {
         StepArgs sp = a;
         sp.nb_dense = 0;
-        if ((r = direct(sp, (a.M + 127) / 128))) return r;
+        if ((r = direct(sp, special_blocks(a)))) return r;
     }
     // a thin first slab lets the copies start early; the rest split evenly.
     // Slab boundaries fall on whole blocks: plane i starts a block when

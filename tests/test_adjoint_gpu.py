@@ -67,6 +67,25 @@ def test_fp64_adjoint_matches_torch_autograd(scheme, zb_name):
     np.testing.assert_allclose(duin, duin_t, rtol=1e-7, atol=1e-9 * np.abs(duin_t).max())
 
 
+def test_fp64_adjoint_rows_of_96_sites():
+    # nz = 96: the reverse kernel's row blocks have 96 threads, and its
+    # boundary-node blocks (the Zou-He inlet and outlet, 2 x 4 x 96 nodes)
+    # must be counted in blocks of 96
+    from jyulb.adjoint import ChannelProblem
+    from jyulb.defs import FIXED_DEN, FIXED_VEL, FP64, PERIODIC, TRT, WALL
+
+    phase, uin, target = setup(4, shape=(10, 4, 96), r=1.0)
+    tau, g, steps, plane = 0.8, np.array([1e-5, 0.0, 0.0]), 14, 7
+    p = ChannelProblem(phase, bc=[FIXED_VEL, FIXED_DEN, WALL, WALL, PERIODIC, PERIODIC], rlx_scheme=TRT,
+                       precision=FP64, trt_magic=0.25, loss_plane=plane, checkpoint_every=5)
+    L, _ = p.forward(tau, g, uin, steps, target)
+    dtau, dg, duin = p.backward()
+    Lt, dtau_t, dg_t, duin_t = torch_grads(phase, tau, g, uin, target, steps, plane, "TRT", 0.25)
+    assert abs(L - Lt) <= 1e-10 * abs(Lt)
+    assert abs(dtau - dtau_t) <= 1e-8 * abs(dtau_t)
+    np.testing.assert_allclose(duin, duin_t, rtol=1e-7, atol=1e-9 * np.abs(duin_t).max())
+
+
 @pytest.mark.parametrize("scheme", [1, 2])
 # FP32: the adjoint of the FP32 model against differences of the FP64 model,
 # so the bound covers both the adjoint and the FP32 model's rounding (measured

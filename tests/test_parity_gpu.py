@@ -276,3 +276,21 @@ def test_mass_conserved_large_periodic():
     # per-site rounding of ~1e-16 per step over 2.6e5 sites and 200 steps
     assert abs(r1["mass"] - r0["mass"]) <= 1e-12 * r0["mass"]
     assert np.allclose(r1["momentum"], r0["momentum"], rtol=0, atol=1e-12 * r0["mass"])
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("bi", [2, 3, 4, 6])
+def test_rows_of_96_sites_with_boundary_nodes(precision, bi):
+    # nz = 96 gives the direct kernel row blocks of 96 threads; its
+    # boundary-node blocks must be counted in blocks of 96 too (Zou-He,
+    # symmetric and moving-wall nodes: several hundred here)
+    c = _random_case(400 + bi, (5, 6, 96), 1, BCSETS[bi], chunks=(3, 4))
+    _, f0, d0, v0 = run_oracle(c)
+    _, f1, d1, v1 = run_engine(c, precision)
+    fl = c["phase"] != 0
+    if precision == 0:
+        np.testing.assert_array_equal(f1[:, fl], f0[:, fl])
+        np.testing.assert_array_equal(v1[fl], v0[fl])
+    else:
+        assert np.abs(f1[:, fl] - f0[:, fl]).max() <= 1e-6
+        assert np.abs(v1[fl] - v0[fl]).max() <= 1e-6
