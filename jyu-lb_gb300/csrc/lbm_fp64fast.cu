@@ -8,11 +8,9 @@
 // (not HBM) bounds the parity step at ~276 separately rounded operations per
 // TRT site:
 //   * den, j and u in the reference's order and rounding,
-//   * the TRT pair relaxation f_q <- c3 f_q - c4 f_opp as one multiply and one
-//     FMA per population,
-//   * the projection of the H10 moments written as one FMA-chain per pair of
-//     opposite populations (even part e, odd part o: f_q += e + o,
-//     f_opp += e - o),
+//   * the projection of the H10 moments grouped per pair of opposite
+//     populations (even part e, odd part o) and merged with the TRT pair
+//     relaxation: f_q <- fma(c3, f_q, fma(-c4, f_opp, e + o)),
 //   * den u formed as j + den a/2 directly,
 // and the unit is compiled with FMA contraction.  Boundary nodes use the
 // reference's Zou-He and Ladd expressions (lbm_fp64.cuh), contracted.
@@ -38,25 +36,45 @@ struct Phys64FBase : Phys64Base {
         return d1x + dx1 + d01y + d0y1 + f[8] + f[9] + f[10];
     }
 
-    // f_q += P(H)_q for H = (H0, H1[3], H2[6]): the reference's 1/72
-    // projection (jyulb/D3Q19.pyx:532-599) regrouped by weight class
-    __device__ static void project_add(const C H0, const C hx, const C hy, const C hz, const C hxx, const C hxy,
-                                       const C hxz, const C hyy, const C hyz, const C hzz, C *f) {
+    // P(H) for H = (H0, H1[3], H2[6]): the reference's 1/72 projection
+    // (jyulb/D3Q19.pyx:532-599) regrouped by weight class and merged with
+    // the pair relaxation: each population becomes
+    //   f_q <- c3 f_q - c4 f_opp + (e +/- o)
+    // as fma(c3, f_q, fma(-c4, f_opp, e +/- o)), one operation fewer per
+    // population than relaxing first and adding the projection after
+    // (BGK: c3 = 1 - w_e, c4 = 0; regularized: c3 = c4 = 0)
+    template <bool PAIR, bool RELAX>
+    __device__ static void relax_project(const C c3, const C c4, const C r9, const C H0, const C hx, const C hy,
+                                         const C hz, const C hxx, const C hxy, const C hxz, const C hyy, const C hyz,
+                                         const C hzz, C *f) {
         const C tr = hxx + hyy + hzz;
         const C A0 = fma(-1.5, tr, H0);
         const C k18 = 1.0 / 18.0, k36 = 1.0 / 36.0, k6 = 1.0 / 6.0, k12 = 1.0 / 12.0;
-        f[9] = fma(A0, 1.0 / 3.0, f[9]);
+        f[9] = RELAX ? fma(A0, 1.0 / 3.0, r9 * f[9]) : A0 * (1.0 / 3.0);
+        auto put = [&](int q, C e, C o) {
+            const C a = f[q], b = f[18 - q];
+            if (!RELAX) {
+                f[q] = e + o;
+                f[18 - q] = e - o;
+            } else if (PAIR) {
+                f[q] = fma(c3, a, fma(-c4, b, e + o));
+                f[18 - q] = fma(c3, b, fma(-c4, a, e - o));
+            } else {
+                f[q] = fma(c3, a, e + o);
+                f[18 - q] = fma(c3, b, e - o);
+            }
+        };
         C e, o;
-        e = fma(4.5, hxx, A0) * k18; o = hx * k6; f[16] += e + o; f[2] += e - o;
-        e = fma(4.5, hyy, A0) * k18; o = hy * k6; f[12] += e + o; f[6] += e - o;
-        e = fma(4.5, hzz, A0) * k18; o = hz * k6; f[10] += e + o; f[8] += e - o;
+        e = fma(4.5, hxx, A0) * k18; o = hx * k6; put(16, e, o);
+        e = fma(4.5, hyy, A0) * k18; o = hy * k6; put(12, e, o);
+        e = fma(4.5, hzz, A0) * k18; o = hz * k6; put(10, e, o);
         const C bxy = fma(4.5, hxx + hyy, A0), bxz = fma(4.5, hxx + hzz, A0), byz = fma(4.5, hyy + hzz, A0);
-        e = fma(9.0, hxy, bxy) * k36; o = (hx + hy) * k12; f[18] += e + o; f[0] += e - o;
-        e = fma(-9.0, hxy, bxy) * k36; o = (hx - hy) * k12; f[14] += e + o; f[4] += e - o;
-        e = fma(9.0, hxz, bxz) * k36; o = (hx + hz) * k12; f[17] += e + o; f[1] += e - o;
-        e = fma(-9.0, hxz, bxz) * k36; o = (hx - hz) * k12; f[15] += e + o; f[3] += e - o;
-        e = fma(9.0, hyz, byz) * k36; o = (hy + hz) * k12; f[13] += e + o; f[5] += e - o;
-        e = fma(-9.0, hyz, byz) * k36; o = (hy - hz) * k12; f[11] += e + o; f[7] += e - o;
+        e = fma(9.0, hxy, bxy) * k36; o = (hx + hy) * k12; put(18, e, o);
+        e = fma(-9.0, hxy, bxy) * k36; o = (hx - hy) * k12; put(14, e, o);
+        e = fma(9.0, hxz, bxz) * k36; o = (hx + hz) * k12; put(17, e, o);
+        e = fma(-9.0, hxz, bxz) * k36; o = (hx - hz) * k12; put(15, e, o);
+        e = fma(9.0, hyz, byz) * k36; o = (hy + hz) * k12; put(13, e, o);
+        e = fma(-9.0, hyz, byz) * k36; o = (hy - hz) * k12; put(11, e, o);
     }
 };
 
@@ -92,9 +110,7 @@ template <int SCH> struct Phys64F : Phys64FBase {
             hxy = fma(c1, pxy, fma(we, sx * uy, c2 * (ax * sy + ay * sx)));
             hxz = fma(c1, pxz, fma(we, sx * uz, c2 * (ax * sz + az * sx)));
             hyz = fma(c1, pyz, fma(we, sy * uz, c2 * (ay * sz + az * sy)));
-#pragma unroll
-            for (int q = 0; q < Q; ++q) f[q] = 0.0;
-            project_add(H0, hx, hy, hz, hxx, hxy, hxz, hyy, hyz, hzz, f);
+            relax_project<false, false>(0.0, 0.0, 0.0, H0, hx, hy, hz, hxx, hxy, hxz, hyy, hyz, hzz, f);
             return den;
         }
         // u = j/den + a/2 as the reference rounds it (no contraction)
@@ -118,19 +134,11 @@ template <int SCH> struct Phys64F : Phys64FBase {
         hyz = fma(we * sy, uz, c2 * (ay * sz + az * sy));
         if (SCH == SCH_BGK) {
             const C r = 1.0 - we;
-#pragma unroll
-            for (int q = 0; q < Q; ++q) f[q] *= r;
+            relax_project<false, true>(r, 0.0, r, H0, hx, hy, hz, hxx, hxy, hxz, hyy, hyz, hzz, f);
         } else {
             const C c3 = 1.0 - 0.5 * (we + wo), c4 = 0.5 * (we - wo);
-#pragma unroll
-            for (int q = 0; q < 9; ++q) {
-                const C a = f[q], b = f[18 - q];
-                f[q] = fma(c3, a, -c4 * b);
-                f[18 - q] = fma(c3, b, -c4 * a);
-            }
-            f[9] *= (1.0 - we);
+            relax_project<true, true>(c3, c4, 1.0 - we, H0, hx, hy, hz, hxx, hxy, hxz, hyy, hyz, hzz, f);
         }
-        project_add(H0, hx, hy, hz, hxx, hxy, hxz, hyy, hyz, hzz, f);
         return den;
     }
 };
