@@ -176,6 +176,11 @@ int launch_step_tma_fp32(const StepArgs &a, int scheme, bool pstep, bool accf, i
 int launch_step_tma_fp16(const StepArgs &a, int scheme, bool pstep, bool accf, int grid, int ntiles, int nsb,
                          int *err, cudaStream_t st);
 int tma_blocks_per_sm_fp32(int scheme);
+// FP16 storage, staged local step with two sites per thread (256-site tiles,
+// nz a multiple of 256; kb2 = nz / 256 tiles per row)
+int launch_step_tma_h2_fp16(const StepArgs &a, int scheme, bool accf, int grid, int ntiles, int kb2, int nsb,
+                            int *err, cudaStream_t st);
+int tma_h2_blocks_per_sm_fp16(int scheme);
 int tma_blocks_per_sm_fp16(int scheme);
 
 } // namespace jlb

@@ -14,6 +14,13 @@ int launch_step_tma_fp16(const StepArgs &a, int scheme, bool pstep, bool accf, i
     return launch_step_tma_impl<StoreF16, PhysH16>(a, scheme, pstep, accf, grid, ntiles, nsb, err, st);
 }
 
+int launch_step_tma_h2_fp16(const StepArgs &a, int scheme, bool accf, int grid, int ntiles, int kb2, int nsb,
+                            int *err, cudaStream_t st) {
+    return launch_step_tma_h2_impl<PhysH16>(a, scheme, accf, grid, ntiles, kb2, nsb, err, st);
+}
+
+int tma_h2_blocks_per_sm_fp16(int scheme) { return tma_h2_blocks_per_sm<PhysH16>(scheme); }
+
 int tma_blocks_per_sm_fp16(int scheme) {
     int nb = 0;
     const size_t smem = 2 * (size_t)TmaGeom<__half>::STAGE * sizeof(__half);

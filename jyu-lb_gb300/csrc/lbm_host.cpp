@@ -660,6 +660,10 @@ int launch_one(jlb_solver *s, const StepArgs &a, bool pstep) {
         const int nb = (int)((a.Nc + 127) / 128) + nsb;
         if (s->prec == PREC_FP32) r = launch_step_sparse_fp32(a, s->cfg.rlx_scheme, pstep, s->accf, nb, s->st);
         else r = launch_step_sparse_fp16(a, s->cfg.rlx_scheme, pstep, s->accf, nb, s->st);
+    } else if (s->use_h2 && !pstep && !a.fout && !a.sp_tee) {
+        const int kb2 = s->nz / 256;
+        r = launch_step_tma_h2_fp16(a, s->cfg.rlx_scheme, s->accf, s->h2_grid, s->nx * s->ny * kb2, kb2, nsb, s->d_err,
+                                    s->st);
     } else if (s->use_tma && !a.fout && !a.sp_tee && (s->tma_p || !pstep)) {
         const int ntiles = a.nb_dense; // one 128-site tile per dense block (bx = 128, by = 1)
         if (s->prec == PREC_FP32)
@@ -688,6 +692,7 @@ int launch_one(jlb_solver *s, const StepArgs &a, bool pstep) {
 // staging, JLB_TMA=1 stages both steps.
 void choose_kernel(jlb_solver *s) {
     s->use_tma = false;
+    s->use_h2 = false;
     // L2 line prefetch 6 blocks per SM ahead (of the 8 resident) on the
     // direct FP32 kernels: 38.8 -> 39.8 GLUPS on the 256^3 cavity, flat from
     // 5 to 8 blocks per SM, worse beyond.  FP16 storage is issue-bound and
@@ -735,6 +740,16 @@ void choose_kernel(jlb_solver *s) {
     }
     s->tma_grid = per_sm * sms;
     s->use_tma = true;
+    // FP16 storage with nz a multiple of 256: the staged local step takes two
+    // sites per thread (JLB_H2=0 keeps one)
+    const char *eh = std::getenv("JLB_H2");
+    if (s->prec == PREC_FP16 && s->nz % 256 == 0 && !(eh && eh[0] == '0')) {
+        const int h2_sm = tma_h2_blocks_per_sm_fp16(s->cfg.rlx_scheme);
+        if (h2_sm > 0) {
+            s->use_h2 = true;
+            s->h2_grid = h2_sm * sms;
+        }
+    }
     ++s->args_version;
 }
 

@@ -101,6 +101,8 @@ struct jlb_solver {
     bool use_tma = false;
     bool tma_p = true; // also for the pull-push step
     int tma_grid = 0;
+    bool use_h2 = false;  // FP16: staged local step with two sites per thread
+    int h2_grid = 0;
     int *d_err = nullptr; // set by a kernel whose bounded wait timed out
     int pf_blocks = 0;    // L2 prefetch distance of the direct step kernel (dense blocks)
     uint64_t args_version = 1, graph_version[2] = {0, 0};

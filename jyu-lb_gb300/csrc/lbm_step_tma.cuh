@@ -228,6 +228,149 @@ __global__ void __launch_bounds__(128, JLB_MIN_BLOCKS_TMA) lbm_step_tma_kernel(c
     for (int sb = blockIdx.x; sb < nspecial_blocks; sb += gridDim.x) special_node<ST, PH, PSTEP, ACCF>(a, sb);
 }
 
+// ---------------------------------------------------------------------------
+// FP16 storage, local step, two consecutive sites per thread.  One 2-byte
+// population per load keeps only half the bytes in flight per register that
+// FP32 does; here each thread takes sites (k, k+1) of a 256-site tile, reads
+// each population of both as one aligned 32-bit word from the staged rows,
+// collides site k and then site k+1 on the stored values (PhysH16), and
+// writes both results of a population with one 32-bit store (one
+// cvt.rn.f16x2.f32 for the pair).  A site that is a boundary node or solid
+// keeps its half: the other half goes out as a 16-bit store.  The rows are
+// staged as in lbm_step_tma_kernel (19 copies of 512 bytes per tile, two
+// buffers, bounded mbarrier waits).  Requires nz a multiple of 256.
+// ---------------------------------------------------------------------------
+struct H2Geom {
+    static constexpr int TW = 256;          // sites per tile (2 per thread)
+    static constexpr int PAD = 8;           // 16 bytes of halves
+    static constexpr int SEG = TW + 2 * PAD; // staged halves per slot
+    static constexpr int STAGE = Q * SEG;   // halves per buffer
+};
+#ifndef JLB_MIN_BLOCKS_H2
+#define JLB_MIN_BLOCKS_H2 6
+#endif
+
+__device__ __forceinline__ void h2_issue(const StepArgs &a, int tile, int kb2, __half *buf, uint64_t *bar) {
+    using G = H2Geom;
+    const int row = tile / kb2;
+    const int k0 = (tile - row * kb2) * G::TW;
+    const __half *f = (const __half *)a.f;
+    constexpr uint32_t nb = G::TW * 2;
+    mbar_arrive_tx(bar, nb * (uint32_t)Q);
+    const int64_t base = (int64_t)row * a.nz + k0;
+#pragma unroll
+    for (int q = 0; q < Q; ++q) bulk_g2s(buf + q * G::SEG + G::PAD, f + (int64_t)q * a.Np + base, nb, bar);
+}
+
+__device__ __forceinline__ void st_h16(__half *p, float v) {
+    *p = __float2half_rn(v);
+}
+
+template <class PH, bool ACCF>
+__global__ void __launch_bounds__(128, JLB_MIN_BLOCKS_H2) lbm_step_tma_h2_kernel(const StepArgs a, int ntiles, int kb2,
+                                                                              int nspecial_blocks, int *err) {
+    using G = H2Geom;
+    using C = float;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    __half *buf0 = (__half *)smem_raw;
+    __half *buf1 = buf0 + G::STAGE;
+    __shared__ __align__(8) uint64_t bar[2];
+    const int t = threadIdx.x;
+    if (t == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+    __half *__restrict__ f = (__half *)a.f;
+    const int32_t Np = (int32_t)a.Np;
+    int tile = blockIdx.x;
+    int it = 0;
+    if (tile < ntiles && t == 0) h2_issue(a, tile, kb2, buf0, &bar[0]);
+    for (; tile < ntiles; tile += gridDim.x, ++it) {
+        const __half *cur = (it & 1) ? buf1 : buf0;
+        const int next = tile + gridDim.x;
+        if (next < ntiles && t == 0) {
+            fence_proxy_async_smem();
+            h2_issue(a, next, kb2, (it & 1) ? buf0 : buf1, &bar[(it + 1) & 1]);
+        }
+        const int row = tile / kb2;
+        const int kA = (tile - row * kb2) * G::TW + 2 * t;
+        const int32_t nA = row * a.nz + kA;
+        // class bytes of both sites in one 16-bit load (nA is even)
+        const uint32_t cl = __ldg((const unsigned short *)(a.ncls + nA));
+        const bool actA = (cl & 0xFFu) < CLS_SPECIAL, actB = (cl >> 8) < CLS_SPECIAL;
+        const bool ok = mbar_wait_bounded(&bar[it & 1], (uint32_t)(it >> 1) & 1u);
+        if (__syncthreads_or(!ok)) {
+            if (t == 0) {
+                atomicExch(err, 1);
+                (void)mbar_wait_bounded(&bar[it & 1], (uint32_t)(it >> 1) & 1u);
+                if (next < ntiles) (void)mbar_wait_bounded(&bar[(it + 1) & 1], (uint32_t)((it + 1) >> 1) & 1u);
+            }
+            __syncthreads();
+            return;
+        }
+        if (actA || actB) {
+            uint32_t w[Q];
+            Unroll<0, Q>::run([&]<int q>() { w[q] = *(const uint32_t *)(cur + q * G::SEG + G::PAD + 2 * t); });
+            C axA, ayA, azA, axB, ayB, azB;
+            if (ACCF) {
+                const C *acc = (const C *)a.acc;
+                axA = (C)a.g[0] + __ldg(acc + nA); axB = (C)a.g[0] + __ldg(acc + nA + 1);
+                ayA = (C)a.g[1] + __ldg(acc + Np + nA); ayB = (C)a.g[1] + __ldg(acc + Np + nA + 1);
+                azA = (C)a.g[2] + __ldg(acc + 2 * Np + nA); azB = (C)a.g[2] + __ldg(acc + 2 * Np + nA + 1);
+            } else {
+                axA = axB = (C)a.g[0]; ayA = ayB = (C)a.g[1]; azA = azB = (C)a.g[2];
+            }
+            C hA[Q], hB[Q];
+            Unroll<0, Q>::run([&]<int q>() { hA[q] = __low2float(*(const __half2 *)&w[q]); });
+            C uxA, uyA, uzA;
+            const C rhoA = PH::collide_h(hA, axA, ayA, azA, (C)a.w_e, (C)a.w_o, uxA, uyA, uzA);
+            Unroll<0, Q>::run([&]<int q>() { hB[q] = __high2float(*(const __half2 *)&w[q]); });
+            C uxB, uyB, uzB;
+            const C rhoB = PH::collide_h(hB, axB, ayB, azB, (C)a.w_e, (C)a.w_o, uxB, uyB, uzB);
+            // local step: population q of both sites goes to slot opp(q)
+            Unroll<0, Q>::run([&]<int q>() {
+                __half *p = f + ((int32_t)OPP(q) * Np + nA);
+                if (actA && actB) *(__half2 *)p = __floats2half2_rn(hA[q], hB[q]);
+                else if (actA) st_h16(p, hA[q]);
+                else st_h16(p + 1, hB[q]);
+            });
+            if (a.write_moments) {
+                C *den = (C *)a.den, *ux = (C *)a.ux, *uy = (C *)a.uy, *uz = (C *)a.uz;
+                if (actA) { den[nA] = rhoA; ux[nA] = uxA; uy[nA] = uyA; uz[nA] = uzA; }
+                if (actB) { den[nA + 1] = rhoB; ux[nA + 1] = uxB; uy[nA + 1] = uyB; uz[nA + 1] = uzB; }
+            }
+        }
+        __syncthreads(); // buffer `cur` is free for the copies issued next round
+    }
+    for (int sb = blockIdx.x; sb < nspecial_blocks; sb += gridDim.x) special_node<StoreF16, PH, false, ACCF>(a, sb);
+}
+
+template <template <int> class PH>
+int launch_step_tma_h2_impl(const StepArgs &a, int scheme, bool accf, int grid, int ntiles, int kb2,
+                            int nspecial_blocks, int *err, cudaStream_t st) {
+    const size_t smem = 2 * (size_t)H2Geom::STAGE * sizeof(__half);
+#define JLB_H(SCH, A) lbm_step_tma_h2_kernel<PH<SCH>, A><<<grid, 128, smem, st>>>(a, ntiles, kb2, nspecial_blocks, err)
+#define JLB_HS(SCH) if (accf) JLB_H(SCH, true); else JLB_H(SCH, false);
+    if (scheme == SCH_BGK) { JLB_HS(SCH_BGK) }
+    else if (scheme == SCH_TRT) { JLB_HS(SCH_TRT) }
+    else { JLB_HS(SCH_REG) }
+#undef JLB_HS
+#undef JLB_H
+    return (int)cudaGetLastError();
+}
+
+template <template <int> class PH> int tma_h2_blocks_per_sm(int scheme) {
+    const size_t smem = 2 * (size_t)H2Geom::STAGE * sizeof(__half);
+    int nb = 0;
+    cudaError_t e;
+    if (scheme == SCH_BGK) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, lbm_step_tma_h2_kernel<PH<SCH_BGK>, false>, 128, smem);
+    else if (scheme == SCH_TRT) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, lbm_step_tma_h2_kernel<PH<SCH_TRT>, false>, 128, smem);
+    else e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, lbm_step_tma_h2_kernel<PH<SCH_REG>, false>, 128, smem);
+    return e == cudaSuccess ? nb : 0;
+}
+
 template <class ST, template <int> class PH>
 int launch_step_tma_impl(const StepArgs &a, int scheme, bool pstep, bool accf, int grid, int ntiles,
                          int nspecial_blocks, int *err, cudaStream_t st) {

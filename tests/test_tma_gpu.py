@@ -71,3 +71,38 @@ def test_staged_fp32_close_to_oracle(bi):
     fl = c["phase"] != 0
     assert np.abs(v[fl] - vo[fl]).max() <= 1e-6
     assert np.abs(f[:, fl] - fo[:, fl]).max() <= 1e-6
+
+
+@pytest.mark.parametrize("bc", [[1, 1, 0, 0, 1, 1], [0, 0, 0, 3, 0, 0], [1, 1, 4, 2, 1, 1]])
+def test_fp16_two_sites_per_thread_local_step(bc):
+    # FP16 storage with nz = 256: the staged local step takes sites (k, k+1)
+    # per thread; 64 x 48 rows = 3072 tiles, several per persistent block, so
+    # both buffers are refilled.  Against the one-site staged kernel
+    # (JLB_H2=0) and the direct kernel; boundary-node and solid sites in a
+    # pair keep their half
+    rng = np.random.default_rng(11)
+    sh = (64, 48, 256)
+    c = dict(lat=list(sh), scheme=1, kvisc=0.04, g=[1e-5, 0.0, 0.0], bc=list(bc), chunks=[9, 4])
+    c["phase"] = (rng.random(sh) < 0.97).astype(np.uint8)
+    c["den0"] = np.ones(sh)
+    v = 0.01 * rng.standard_normal(sh + (3,))
+    v[c["phase"] == 0] = 0.0
+    if bc[3] == 3:
+        v[:, -1, :, 0] = 0.04
+    c["vel0"] = v
+    c["acc0"] = None
+    fl = c["phase"] != 0
+    _, f2, _, v2 = _run(c, 2, "L")
+    old = os.environ.get("JLB_H2")
+    os.environ["JLB_H2"] = "0"
+    try:
+        _, f1, _, v1 = _run(c, 2, "L")
+    finally:
+        if old is None:
+            del os.environ["JLB_H2"]
+        else:
+            os.environ["JLB_H2"] = old
+    _, f0, _, v0 = _run(c, 2, False)
+    for f, v in ((f1, v1), (f0, v0)):
+        np.testing.assert_allclose(f2[:, fl], f[:, fl], rtol=0, atol=2e-5)
+        np.testing.assert_allclose(v2[fl], v[fl], rtol=0, atol=2e-5)
