@@ -296,8 +296,8 @@ void jlb_rlx_prm(const jlb_solver *s, double out[2]);
 /* number of kernel launches issued by this solver so far */
 uint64_t jlb_kernel_launches(const jlb_solver *s);
 
-/* cumulative wall-clock seconds of jlb_evolve's phases: out[0] halo rules and
- * solid-velocity check, out[1] Zou-He / boundary-node inputs, out[2]
+/* cumulative wall-clock seconds of jlb_evolve's phases: out[0] bc-data copy,
+ * halo rules and solid-velocity check, out[1] Zou-He / boundary-node inputs, out[2]
  * acceleration field, out[3] step launches, out[4] step completion and the
  * den/vel download, out[5] whole calls */
 void jlb_host_timers(const jlb_solver *s, double out[6]);

@@ -705,8 +705,16 @@ void choose_kernel(jlb_solver *s) {
             cudaGetLastError();
             sms = 0;
         }
+        // only where the populations do not stay in L2 between steps (a
+        // lattice that fits gains nothing and pays for the instructions)
+        int l2 = 0;
+        if (cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, dev) != cudaSuccess) {
+            cudaGetLastError();
+            l2 = 0;
+        }
+        const bool big = (double)19 * (double)s->Np * (double)s->ssz > 2.0 * (double)l2;
         const char *ep = std::getenv("JLB_PF");
-        s->pf_blocks = (ep && ep[0]) ? std::max(0, std::atoi(ep)) : (s->prec == PREC_FP32 ? 6 * sms : 0);
+        s->pf_blocks = (ep && ep[0]) ? std::max(0, std::atoi(ep)) : (s->prec == PREC_FP32 && big ? 6 * sms : 0);
         ++s->args_version;
     }
     // fluid-only layout for FP32 / FP16 storage when under 80% of the sites
@@ -1378,8 +1386,12 @@ int jlb_evolve(jlb_solver *s, uint32_t tsteps, const double g[3], double *den, d
     if (!s) return fail(s, JLB_ERR_INVALID_ARG, "NULL solver");
     if (!den || !vel) return fail(s, JLB_ERR_INVALID_ARG, "NULL den/vel");
     // the reference copies the bc data first, before its own checks and halo
-    // rules (jyulb/isothermal.pyx:1398)
-    snapshot_bc_data(s, den, vel);
+    // rules (jyulb/isothermal.pyx:1398); counted in host phase 0
+    {
+        const auto t_bc = std::chrono::steady_clock::now();
+        snapshot_bc_data(s, den, vel);
+        s->host_t[0] += std::chrono::duration<double>(std::chrono::steady_clock::now() - t_bc).count();
+    }
     if (!s->init_done)
         return fail(s, JLB_ERR_STATE, "Finalize solver initialization before calling evolve\n"
                                       "(i.e. call first the method finalize_init)!");
