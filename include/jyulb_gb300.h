@@ -250,8 +250,11 @@ const char *jlb_batch_last_error(const jlb_batch *b);
 /* ---------------------------------------------------------------------
  * Discrete adjoint of the time step (no counterpart in the reference, which
  * has no derivatives).  A problem is a domain described by a jlb_config:
- * BGK, TRT or regularized, FP64 or FP32, started from rest; its parameters are the relaxation time
- * tau, the body force g and the u_x of each site of a FIXED_VEL face 1X.
+ * BGK, TRT or regularized, FP64 or FP32, started from rest, with immobile or
+ * moving solids; its parameters are the relaxation time tau, the body force g
+ * and the Zou-He data of its fixed faces (jlb_adj_forward: the u_x of each
+ * site of a FIXED_VEL face 1X; jlb_adj_forward_fields: den and vel of every
+ * boundary site of any fixed face).
  * The loss is sum |u - target|^2 of the stored velocity on the plane
  * x = loss_plane after the last step.  The forward run keeps checkpoints
  * every checkpoint_every steps; the backward run recomputes each segment and
@@ -268,6 +271,25 @@ int jlb_adj_forward(jlb_adjoint *a, double tau, const double g[3], const double 
                     uint32_t steps, const double *target, double *loss, double *u_plane);
 /* gradients of the last forward run's loss; duin: (ny,nz) */
 int jlb_adj_backward(jlb_adjoint *a, double *dtau, double dg[3], double *duin);
+/* As jlb_adj_create, with moving solids: solid_vel (nx,ny,nz,3) is read at
+ * the solid sites, like Solver.vel at phase == SOLID, and enters the links
+ * into them through Ladd's term 6 w_q den_prev (c_q . u_wall)
+ * (jyulb/isothermal.pyx:1112-1248); the reverse sweep carries the adjoint of
+ * each boundary site's previous-step density. */
+int jlb_adj_create_moving(const jlb_config *cfg, const uint8_t *phase, const double *solid_vel, int32_t loss_plane,
+                          int32_t checkpoint_every, jlb_adjoint **out);
+/* Forward run whose Zou-He data come from den (nx,ny,nz) and vel (nx,ny,nz,3)
+ * at the boundary sites, as Solver.evolve reads them
+ * (jyulb/isothermal.pyx:476-502): every FIXED_VEL and FIXED_DEN face, any of
+ * the six; Z1 only when bc[Z1] is FIXED_DEN or bc[1Z] is FIXED_VEL (:500), the
+ * others keep den 1, vel 0.  NULL den or vel: 1 or 0 everywhere. */
+int jlb_adj_forward_fields(jlb_adjoint *a, double tau, const double g[3], const double *den, const double *vel,
+                           uint32_t steps, const double *target, double *loss, double *u_plane);
+/* gradients of the last forward run's loss w.r.t. tau, g and the den / vel
+ * values its Zou-He faces read (zero elsewhere); dden (nx,ny,nz), dvel
+ * (nx,ny,nz,3), either may be NULL.  After jlb_adj_forward, the face-1X
+ * u_x entries carry duin and the rest is zero. */
+int jlb_adj_backward_fields(jlb_adjoint *a, double *dtau, double dg[3], double *dden, double *dvel);
 /* device time (ms, CUDA events on the problem's stream) of the last runs:
  * out[0] forward, out[1] recomputation, out[2] reverse sweep, out[3] the
  * whole backward run */

@@ -101,11 +101,12 @@ __device__ __forceinline__ int axcomp(int q, int ax) { return ax == 0 ? CX(q) : 
 
 // Transposed Zou-He at a face node.  gp: the populations after Zou-He (the
 // known ones equal the pre-Zou-He values), mu: adjoint w.r.t. gp; returns in
-// mu the adjoint w.r.t. the pre-Zou-He populations and adds du (adjoint of the
-// boundary velocity) for a FIXED_VEL face.
+// mu the adjoint w.r.t. the pre-Zou-He populations and adds the adjoint of the
+// face data: du (boundary velocity; a FIXED_DEN face uses its tangential
+// components) and dden (density of a FIXED_DEN face).
 template <class C, bool SHIFTED>
 __device__ void zh_adjoint(int fc, int kind, double den, double ux, double uy, double uz, const C *gp, C *mu,
-                           double *du) {
+                           double *du, double &dden) {
     const int ax = fc >> 1;
     const bool high = fc & 1;
     const int in_sign = high ? -1 : 1; // normal component of the unknown populations
@@ -154,8 +155,14 @@ __device__ void zh_adjoint(int fc, int kind, double den, double ux, double uy, d
         for (int a = 0; a < 3; ++a) du[a] += rho_bc * (double)dj[a];
         du[ax] += dju * (high ? -rho_bc / denom : rho_bc / denom);
     } else {
-        // j_n = +/-(S - den), j_t = den u_t
+        // j_n = den - S on a low face, S - den on a high one; j_t = den u_t
         dS = high ? dj[ax] : -dj[ax];
+        dden += high ? -(double)dj[ax] : (double)dj[ax];
+        for (int t = 0; t < 3; ++t) {
+            if (t == ax) continue;
+            dden += (double)dj[t] * u[t];
+            du[t] += den * (double)dj[t];
+        }
     }
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
@@ -450,6 +457,13 @@ __device__ __forceinline__ void adjoint_boundary_sites(const AdjArgs &A, int b, 
         adj_accumulate(sums, g, lo);
         adj_finish<C, ST::shifted, SCH, SEED>(sums, lo, (C)a.g[0], (C)a.g[1], (C)a.g[2], (C)a.w_e, (C)a.w_o, pg, on_plane,
                                              tg, a.g[0], a.g[1], a.g[2], [&]<int q>(C v) { li[q] = v; });
+        C *lam_den = (C *)A.lam_den;
+        if (lam_den) {
+            // the density this step stored for the next step's moving-wall
+            // links is the sum of the collision inputs
+            const C ld = lam_den[t];
+            Unroll<0, Q>::run([&]<int q>() { li[q] += ld; });
+        }
         const uint32_t info = __ldg(a.sp_info + t);
         const uint32_t faces = (info >> SP_FACE_SHIFT) & 0x3Fu;
         // faces were applied in increasing order, so transpose in decreasing
@@ -459,11 +473,24 @@ __device__ __forceinline__ void adjoint_boundary_sites(const AdjArgs &A, int b, 
         for (int fc = 5; fc >= 0; --fc) {
             if (!(faces & (1u << fc))) continue;
             const double *bcd = a.sp_bc + (int64_t)(4 * slots[fc]) * M + t;
-            double du[3] = {0, 0, 0};
+            double du[3] = {0, 0, 0}, dden = 0.0;
             zh_adjoint<C, ST::shifted>(fc, a.bc[fc], bcd[0], bcd[M], bcd[2 * (int64_t)M], bcd[3 * (int64_t)M], g,
-                                       li, du);
-            // one boundary site per inlet (j, k): a plain add is race-free
-            if (fc == 0 && a.bc[0] == BC_FIXED_VEL && A.grad_uin) A.grad_uin[(int64_t)j * a.nz + k] += du[0];
+                                       li, du, dden);
+            // one thread per boundary site: plain adds are race-free
+            if (A.grad_bc && ((A.param_faces >> fc) & 1u)) {
+                A.grad_bc[t] += dden;
+                for (int c = 0; c < 3; ++c) A.grad_bc[(int64_t)(1 + c) * M + t] += du[c];
+            }
+        }
+        if (lam_den) {
+            // Ladd's term of a moving link, g_q = f + 6 w_q den_prev (c_q . u_wall),
+            // passes its adjoint to the density of the previous step
+            C ld = 0;
+            Unroll<0, Q>::run([&]<int q>() {
+                if (q != 9 && (info & (1u << q)))
+                    ld += li[q] * (C)(6.0 * WQ<q>()) * (C)__ldg(a.sp_lw + (int64_t)q * M + t);
+            });
+            lam_den[t] = ld;
         }
         Unroll<0, Q>::run([&]<int q>() {
             const int64_t r = PSTEP ? __ldg(a.sp_rd + (int64_t)q * M + t) : (int64_t)q * Np + n;

@@ -17,7 +17,12 @@ struct AdjArgs {
     const double *target;  // (ny, nz, 3) target velocity on the plane
     double *part;          // [adjoint_blocks][5] per-block sums of d/d we, d/d wo,
                            // d/d a_x, a_y, a_z (accumulated over the sweep)
-    double *grad_uin;      // [ny*nz] d/d u_x of the FIXED_VEL face 1X (accumulated)
+    double *grad_bc;       // [4][M] d/d (den, ux, uy, uz) of each boundary site's Zou-He
+                           // data (accumulated), or NULL
+    uint32_t param_faces;  // faces (bit f = face f) whose Zou-He data are parameters
+    void *lam_den;         // [M] adjoint of each boundary site's density of the step
+                           // (compute type; read by the next step's moving-wall
+                           // links), or NULL when no link moves
 };
 
 // one step of the reverse sweep (one launch)

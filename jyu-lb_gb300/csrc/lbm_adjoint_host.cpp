@@ -6,6 +6,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <functional>
 #include <string>
 #include <vector>
 
@@ -33,7 +34,16 @@ struct jlb_adjoint {
     int nsets = 0;
     cudaStream_t st2 = nullptr; // recompute stream
     void *lam = nullptr;
-    double *d_target = nullptr, *d_part = nullptr, *d_guin = nullptr;
+    double *d_target = nullptr, *d_part = nullptr;
+    double *d_gbc = nullptr;      // [4][M] d/d (den, ux, uy, uz) of the boundary sites' Zou-He data
+    // previous-step density of the boundary sites (compute type; den - 1 when
+    // shifted), which the moving-wall links read: at rest, at each checkpoint
+    // ([segment][M]), and the recompute's working copy
+    void *spd0 = nullptr, *ckpt_spd = nullptr, *spd_scratch = nullptr;
+    int ckpt_spd_cap = 0;         // segments ckpt_spd holds
+    void *lam_den = nullptr;      // [M] adjoint of the boundary sites' density
+    bool moving = false;          // some boundary site has a moving-wall link
+    uint32_t param_faces = 0;     // faces whose Zou-He data the last forward run took as parameters
     int nparts = 0;           // per-block sensitivity slots
     uint32_t steps = 0;
     double tau = 1.0;
@@ -96,14 +106,19 @@ void jlb_adj_destroy(jlb_adjoint *A) {
     for (void *p : A->ckpt) if (p) cudaFree(p);
     for (void *p : A->snap) if (p) cudaFree(p);
     for (cudaEvent_t e : A->ev) cudaEventDestroy(e);
-    void *bufs[] = {A->f0, A->lam, A->sp_in, A->d_target, A->d_part, A->d_guin};
+    void *bufs[] = {A->f0, A->lam, A->sp_in, A->d_target, A->d_part, A->d_gbc,
+                    A->spd0, A->ckpt_spd, A->spd_scratch, A->lam_den};
     for (void *p : bufs) if (p) cudaFree(p);
     if (A->s) jlb_destroy(A->s);
     delete A;
 }
 
-int jlb_adj_create(const jlb_config *cfg, const uint8_t *phase, int32_t loss_plane, int32_t checkpoint_every,
-                   jlb_adjoint **out) {
+}  // extern "C"
+
+namespace {
+
+int adj_create(const jlb_config *cfg, const uint8_t *phase, const double *solid_vel, int32_t loss_plane,
+               int32_t checkpoint_every, jlb_adjoint **out) {
     jlb_adjoint *A = nullptr;
     if (!cfg || !phase || !out) return afail(nullptr, JLB_ERR_INVALID_ARG, "NULL argument");
     *out = nullptr;
@@ -112,11 +127,6 @@ int jlb_adj_create(const jlb_config *cfg, const uint8_t *phase, int32_t loss_pla
     if (checkpoint_every < 1) return afail(nullptr, JLB_ERR_INVALID_ARG, "checkpoint interval must be >= 1");
     if (cfg->kernel != JLB_KERNEL_JYULB)
         return afail(nullptr, JLB_ERR_UNSUPPORTED, "adjoint supports the jyulb collision kernel");
-    for (int f = 1; f < 6; ++f)
-        if (cfg->bc[f] == JLB_FIXED_VEL)
-            return afail(nullptr, JLB_ERR_UNSUPPORTED, "adjoint: FIXED_VEL is supported on face 1X only");
-    if (cfg->bc[0] == JLB_FIXED_VEL && cfg->bc[1] != JLB_PERIODIC && cfg->lat_size[0] == 1)
-        return afail(nullptr, JLB_ERR_UNSUPPORTED, "adjoint: a one-site-thick domain with two Zou-He faces");
     if (loss_plane < 0 || loss_plane >= cfg->lat_size[0]) return afail(nullptr, JLB_ERR_INVALID_ARG, "loss plane out of range");
     A = new jlb_adjoint();
     A->K = checkpoint_every;
@@ -127,14 +137,20 @@ int jlb_adj_create(const jlb_config *cfg, const uint8_t *phase, int32_t loss_pla
     jlb_solver *s = A->s;
     s->no_sparse = true;  // checkpoints and recomputation work on the lattice layout
     s->no_lin = true;
-    // rest state: den = 1, vel = 0 everywhere, so the initial populations do
-    // not depend on the parameters
+    // rest state: den = 1, vel = 0 at the fluid sites, so the initial
+    // populations do not depend on the parameters; solid sites carry their
+    // wall velocity (moving bounce-back with Ladd's term)
     std::vector<uint8_t> ph((size_t)s->NCNT, 0);
     std::vector<double> den((size_t)s->NCNT, 1.0), vel(3 * (size_t)s->NCNT, 0.0);
     for (int i = 0; i < s->nx; ++i)
         for (int j = 0; j < s->ny; ++j)
-            for (int k = 0; k < s->nz; ++k)
-                ph[fidx(s, i + 1, j + 1, k + 1)] = phase[((size_t)i * s->ny + j) * s->nz + k];
+            for (int k = 0; k < s->nz; ++k) {
+                const size_t n = ((size_t)i * s->ny + j) * s->nz + k;
+                const int64_t fn = fidx(s, i + 1, j + 1, k + 1);
+                ph[fn] = phase[n];
+                if (solid_vel && phase[n] == 0)
+                    for (int c = 0; c < 3; ++c) vel[3 * fn + c] = solid_vel[3 * n + c];
+            }
     uint64_t nf = 0;
     if ((r = jlb_finalize_init(s, ph.data(), den.data(), vel.data(), &nf))) {
         std::string m = s->err;
@@ -144,26 +160,41 @@ int jlb_adj_create(const jlb_config *cfg, const uint8_t *phase, int32_t loss_pla
     A->fbytes = (size_t)19 * s->Np * s->ssz;
     auto bail = [&](const char *m) { jlb_adj_destroy(A); return afail(nullptr, JLB_ERR_NOMEM, m); };
     if (cudaMalloc(&A->f0, A->fbytes) != cudaSuccess || cudaMalloc(&A->lam, A->fbytes) != cudaSuccess ||
-        cudaMalloc(&A->d_target, 3 * sizeof(double) * (size_t)s->ny * s->nz) != cudaSuccess ||
-        cudaMalloc(&A->d_guin, sizeof(double) * (size_t)s->ny * s->nz) != cudaSuccess) {
+        cudaMalloc(&A->d_target, 3 * sizeof(double) * (size_t)s->ny * s->nz) != cudaSuccess) {
         cudaGetLastError();
         return bail("adjoint state allocation failed");
     }
     A->nparts = adjoint_blocks(make_args(s, 0));
+    const size_t M1 = (size_t)std::max(s->M, 1);
     if (cudaMalloc(&A->d_part, 5 * sizeof(double) * (size_t)A->nparts) != cudaSuccess ||
         (s->M > 0 && cudaMalloc(&A->sp_in, (size_t)2 * A->K * 19 * s->M * s->ssz) != cudaSuccess) ||
+        cudaMalloc(&A->d_gbc, 4 * sizeof(double) * M1) != cudaSuccess ||
+        cudaMalloc(&A->spd0, M1 * s->csz) != cudaSuccess || cudaMalloc(&A->spd_scratch, M1 * s->csz) != cudaSuccess ||
+        cudaMalloc(&A->lam_den, M1 * s->csz) != cudaSuccess ||
         cudaStreamCreateWithFlags(&A->st2, cudaStreamNonBlocking) != cudaSuccess) {
         cudaGetLastError();
         return bail("adjoint state allocation failed");
     }
+    // density 1 at rest: 1.0 in FP64, den - 1 = 0 in the shifted FP32 form
+    if (s->prec == PREC_FP64) {
+        std::vector<double> one(M1, 1.0);
+        cudaMemcpy(A->spd0, one.data(), M1 * sizeof(double), cudaMemcpyHostToDevice);
+    } else {
+        cudaMemset(A->spd0, 0, M1 * s->csz);
+    }
+    for (int t = 0; t < s->M; ++t)
+        if (s->sp_info[t] & ((1u << 19) - 1u)) A->moving = true;
     cudaMemcpy(A->f0, s->f, A->fbytes, cudaMemcpyDeviceToDevice);
     *out = A;
     return JLB_OK;
 }
 
-int jlb_adj_forward(jlb_adjoint *A, double tau, const double g[3], const double *uin, double rho_out, uint32_t steps,
-                    const double *target, double *loss, double *u_plane) {
-    if (!A || !g || !uin || steps < 1) return afail(A, JLB_ERR_INVALID_ARG, "bad argument");
+// Zou-He data of boundary site t on face `face`: out = (den, ux, uy, uz)
+using BcFill = std::function<void(int t, int face, int64_t n, double *out)>;
+
+int adj_forward(jlb_adjoint *A, double tau, const double g[3], const BcFill &fill, uint32_t param_faces,
+                uint32_t steps, const double *target, double *loss, double *u_plane) {
+    if (!A || !g || steps < 1) return afail(A, JLB_ERR_INVALID_ARG, "bad argument");
     if (!(tau > 0.5)) return afail(A, JLB_ERR_INVALID_ARG, "tau must exceed 1/2");
     jlb_solver *s = A->s;
     double we, wo;
@@ -172,33 +203,41 @@ int jlb_adj_forward(jlb_adjoint *A, double tau, const double g[3], const double 
     s->wo = wo;
     for (int d = 0; d < 3; ++d) s->g[d] = g[d];
     ++s->args_version;
-    // Zou-He data: inlet 1X velocity (uin[j*nz+k], 0, 0), outlet density rho_out
+    // Zou-He data of the boundary sites, in the forward step's slot order
     const int M = s->M;
     const size_t nb = 4 * (size_t)std::max(s->bc_slots, 1) * M;
     std::vector<double> bc(nb, 0.0);
     for (int t = 0; t < M; ++t) {
         const int64_t n = s->sp_node[t];
-        const int j = (int)((n / s->nz) % s->ny), k = (int)(n % s->nz);
         const uint32_t faces = (s->sp_info[t] >> SP_FACE_SHIFT) & 0x3Fu;
         int slot = 0;
         for (int face = 0; face < 6; ++face) {
             if (!(faces & (1u << face))) continue;
-            const bool vel_face = s->cfg.bc[face] == JLB_FIXED_VEL;
-            bc[(size_t)(4 * slot) * M + t] = vel_face ? 1.0 : rho_out;
-            bc[(size_t)(4 * slot + 1) * M + t] = vel_face ? uin[(size_t)j * s->nz + k] : 0.0;
+            double d[4] = {1.0, 0.0, 0.0, 0.0};
+            fill(t, face, n, d);
+            for (int c = 0; c < 4; ++c) bc[(size_t)(4 * slot + c) * M + t] = d[c];
             slot = 1;
         }
     }
+    const int nseg = (int)((steps + A->K - 1) / A->K);
     if (M > 0) {
         ACK(cudaMemcpyAsync(s->d_sp_bc, bc.data(), nb * sizeof(double), cudaMemcpyHostToDevice, s->st));
-        ACK(cudaMemsetAsync(s->d_sp_den, 0, (size_t)M * s->csz, s->st));
+        ACK(cudaMemcpyAsync(s->d_sp_den, A->spd0, (size_t)M * s->csz, cudaMemcpyDeviceToDevice, s->st));
+        if (A->ckpt_spd_cap < nseg) {
+            ACK(cudaStreamSynchronize(s->st));
+            if (A->ckpt_spd) cudaFree(A->ckpt_spd);
+            A->ckpt_spd = nullptr;
+            A->ckpt_spd_cap = 0;
+            ACK(cudaMalloc(&A->ckpt_spd, (size_t)nseg * M * s->csz));
+            A->ckpt_spd_cap = nseg;
+        }
     }
+    A->param_faces = param_faces;
     // forward with checkpoints
     ACK(adj_events(A, 2));
     ACK(cudaEventRecord(A->ev[0], s->st));
     ACK(cudaMemcpyAsync(s->f, A->f0, A->fbytes, cudaMemcpyDeviceToDevice, s->st));
     s->parity = 0;
-    const int nseg = (int)((steps + A->K - 1) / A->K);
     while ((int)A->ckpt.size() < nseg) {
         void *p = nullptr;
         ACK(cudaMalloc(&p, A->fbytes));
@@ -206,6 +245,9 @@ int jlb_adj_forward(jlb_adjoint *A, double tau, const double g[3], const double 
     }
     for (int seg = 0; seg < nseg; ++seg) {
         ACK(cudaMemcpyAsync(A->ckpt[seg], s->f, A->fbytes, cudaMemcpyDeviceToDevice, s->st));
+        if (M > 0)
+            ACK(cudaMemcpyAsync((char *)A->ckpt_spd + (size_t)seg * M * s->csz, s->d_sp_den, (size_t)M * s->csz,
+                                cudaMemcpyDeviceToDevice, s->st));
         const uint32_t t0 = (uint32_t)seg * A->K, t1 = std::min<uint32_t>(steps, t0 + A->K);
         int r = run_steps(s, t1 - t0, t1 == steps);
         if (r) return afail(A, r, s->err);
@@ -251,7 +293,9 @@ int jlb_adj_forward(jlb_adjoint *A, double tau, const double g[3], const double 
     return JLB_OK;
 }
 
-int jlb_adj_backward(jlb_adjoint *A, double *dtau, double dg[3], double *duin) {
+// the reverse sweep; leaves d/d (den, ux, uy, uz) of the boundary sites'
+// Zou-He data in gbc ([4][M], host)
+int adj_backward(jlb_adjoint *A, double *dtau, double dg[3], std::vector<double> &gbc) {
     if (!A) return afail(A, JLB_ERR_INVALID_ARG, "NULL adjoint");
     if (!A->have_forward) return afail(A, JLB_ERR_STATE, "run jlb_adj_forward first");
     jlb_solver *s = A->s;
@@ -284,7 +328,9 @@ int jlb_adj_backward(jlb_adjoint *A, double *dtau, double dg[3], double *duin) {
     ACK(cudaEventRecord(ev[2], st));
     ACK(cudaMemsetAsync(A->lam, 0, A->fbytes, st));
     ACK(cudaMemsetAsync(A->d_part, 0, 5 * sizeof(double) * (size_t)A->nparts, st));
-    ACK(cudaMemsetAsync(A->d_guin, 0, sizeof(double) * (size_t)s->ny * s->nz, st));
+    const size_t M1 = (size_t)std::max(s->M, 1);
+    ACK(cudaMemsetAsync(A->d_gbc, 0, 4 * sizeof(double) * M1, st));
+    ACK(cudaMemsetAsync(A->lam_den, 0, M1 * s->csz, st));
     ACK(cudaStreamWaitEvent(st2, ev[2], 0)); // checkpoints of the forward run are complete
     const size_t sp_step = (size_t)19 * s->M * s->ssz; // bytes of one step's boundary-site inputs
     auto seg_ev = [&](int seg) { return ev + 4 + 4 * (size_t)seg; }; // rc start, rc end, rv start, rv end
@@ -306,8 +352,12 @@ int jlb_adj_backward(jlb_adjoint *A, double *dtau, double dg[3], double *duin) {
         uint32_t t0, t1;
         range(seg, t0, t1);
         ACK(cudaEventRecord(seg_ev(seg)[0], st2));
+        if (s->M > 0)
+            ACK(cudaMemcpyAsync(A->spd_scratch, (char *)A->ckpt_spd + (size_t)seg * s->M * s->csz,
+                                (size_t)s->M * s->csz, cudaMemcpyDeviceToDevice, st2));
         for (uint32_t t = t0; t < t1; ++t) {
             StepArgs a = make_args(s, 0);
+            a.sp_den = A->spd_scratch;
             a.f = state_before(seg, t);
             a.fout = t + 1 < t1 ? state_before(seg, t + 1) : A->snap[(size_t)(seg % nsets) * K];
             a.sp_tee = sp_in_of(seg, t);
@@ -340,7 +390,9 @@ int jlb_adj_backward(jlb_adjoint *A, double *dtau, double dg[3], double *duin) {
             a.plane = A->plane;
             a.target = A->d_target;
             a.part = A->d_part;
-            a.grad_uin = A->d_guin;
+            a.grad_bc = A->d_gbc;
+            a.param_faces = A->param_faces;
+            a.lam_den = A->moving ? A->lam_den : nullptr;
             r = launch_adjoint_step(a, s->prec, s->cfg.rlx_scheme, (t & 1) == 0, st);
             if (r) return afail(A, JLB_ERR_CUDA, std::string("adjoint step: ") + cudaGetErrorString((cudaError_t)r));
             s->launches += 2;
@@ -356,7 +408,8 @@ int jlb_adj_backward(jlb_adjoint *A, double *dtau, double dg[3], double *duin) {
     ACK(cudaEventRecord(ev[3], st));
     std::vector<double> part(5 * (size_t)A->nparts);
     ACK(cudaMemcpyAsync(part.data(), A->d_part, part.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
-    if (duin) ACK(cudaMemcpyAsync(duin, A->d_guin, sizeof(double) * (size_t)s->ny * s->nz, cudaMemcpyDeviceToHost, st));
+    gbc.assign(4 * M1, 0.0);
+    ACK(cudaMemcpyAsync(gbc.data(), A->d_gbc, 4 * sizeof(double) * M1, cudaMemcpyDeviceToHost, st));
     ACK(cudaStreamSynchronize(st));
     double gr[5] = {0, 0, 0, 0, 0};
     for (int b = 0; b < A->nparts; ++b)
@@ -380,6 +433,98 @@ int jlb_adj_backward(jlb_adjoint *A, double *dtau, double dg[3], double *duin) {
         else *dtau = (gr[0] + gr[1]) * (-we * we);
     }
     if (dg) for (int d = 0; d < 3; ++d) dg[d] = gr[2 + d];
+    return JLB_OK;
+}
+
+// faces whose data the solver refreshes from the den / vel fields at every
+// call (the fixed faces; Z1 only when bc[Z1] is FIXED_DEN or bc[1Z] is
+// FIXED_VEL, jyulb/isothermal.pyx:500)
+uint32_t refreshed_faces(const jlb_solver *s) {
+    uint32_t m = 0;
+    for (int f = 0; f < 6; ++f) {
+        bool r = s->cfg.bc[f] == JLB_FIXED_VEL || s->cfg.bc[f] == JLB_FIXED_DEN;
+        if (f == 5) r = s->cfg.bc[5] == JLB_FIXED_DEN || s->cfg.bc[4] == JLB_FIXED_VEL;
+        if (r) m |= 1u << f;
+    }
+    return m;
+}
+
+} // namespace
+
+extern "C" {
+
+int jlb_adj_create(const jlb_config *cfg, const uint8_t *phase, int32_t loss_plane, int32_t checkpoint_every,
+                   jlb_adjoint **out) {
+    return adj_create(cfg, phase, nullptr, loss_plane, checkpoint_every, out);
+}
+
+int jlb_adj_create_moving(const jlb_config *cfg, const uint8_t *phase, const double *solid_vel, int32_t loss_plane,
+                          int32_t checkpoint_every, jlb_adjoint **out) {
+    if (!solid_vel) return afail(nullptr, JLB_ERR_INVALID_ARG, "NULL solid velocity");
+    return adj_create(cfg, phase, solid_vel, loss_plane, checkpoint_every, out);
+}
+
+int jlb_adj_forward(jlb_adjoint *A, double tau, const double g[3], const double *uin, double rho_out, uint32_t steps,
+                    const double *target, double *loss, double *u_plane) {
+    if (!A || !uin) return afail(A, JLB_ERR_INVALID_ARG, "bad argument");
+    const jlb_solver *s = A->s;
+    for (int f = 1; f < 6; ++f)
+        if (s->cfg.bc[f] == JLB_FIXED_VEL)
+            return afail(A, JLB_ERR_UNSUPPORTED, "jlb_adj_forward: FIXED_VEL on a face other than 1X needs jlb_adj_forward_fields");
+    // inlet 1X velocity (uin[j*nz+k], 0, 0), density rho_out on FIXED_DEN faces
+    const BcFill fill = [&](int, int face, int64_t n, double *d) {
+        if (s->cfg.bc[face] == JLB_FIXED_VEL) {
+            d[1] = uin[(size_t)(n % ((int64_t)s->ny * s->nz))];
+        } else {
+            d[0] = rho_out;
+        }
+    };
+    const uint32_t pf = s->cfg.bc[0] == JLB_FIXED_VEL ? 1u : 0u;
+    return adj_forward(A, tau, g, fill, pf, steps, target, loss, u_plane);
+}
+
+int jlb_adj_forward_fields(jlb_adjoint *A, double tau, const double g[3], const double *den, const double *vel,
+                           uint32_t steps, const double *target, double *loss, double *u_plane) {
+    if (!A) return afail(A, JLB_ERR_INVALID_ARG, "NULL adjoint");
+    const jlb_solver *s = A->s;
+    const uint32_t pf = refreshed_faces(s);
+    const BcFill fill = [&](int, int face, int64_t n, double *d) {
+        if (!((pf >> face) & 1u)) return; // den 1, vel 0
+        if (den) d[0] = den[n];
+        if (vel) for (int c = 0; c < 3; ++c) d[1 + c] = vel[3 * n + c];
+    };
+    return adj_forward(A, tau, g, fill, pf, steps, target, loss, u_plane);
+}
+
+int jlb_adj_backward(jlb_adjoint *A, double *dtau, double dg[3], double *duin) {
+    std::vector<double> gbc;
+    const int r = adj_backward(A, dtau, dg, gbc);
+    if (r || !duin) return r;
+    const jlb_solver *s = A->s;
+    const size_t M1 = (size_t)std::max(s->M, 1);
+    std::fill(duin, duin + (size_t)s->ny * s->nz, 0.0);
+    if (s->cfg.bc[0] == JLB_FIXED_VEL)
+        for (int t = 0; t < s->M; ++t)
+            if ((s->sp_info[t] >> SP_FACE_SHIFT) & 1u) {
+                const int64_t n = s->sp_node[t];
+                duin[(size_t)(n % ((int64_t)s->ny * s->nz))] += gbc[M1 + t];
+            }
+    return JLB_OK;
+}
+
+int jlb_adj_backward_fields(jlb_adjoint *A, double *dtau, double dg[3], double *dden, double *dvel) {
+    std::vector<double> gbc;
+    const int r = adj_backward(A, dtau, dg, gbc);
+    if (r) return r;
+    const jlb_solver *s = A->s;
+    const size_t M1 = (size_t)std::max(s->M, 1);
+    if (dden) std::fill(dden, dden + (size_t)s->N, 0.0);
+    if (dvel) std::fill(dvel, dvel + 3 * (size_t)s->N, 0.0);
+    for (int t = 0; t < s->M; ++t) {
+        const int64_t n = s->sp_node[t];
+        if (dden) dden[n] += gbc[t];
+        if (dvel) for (int c = 0; c < 3; ++c) dvel[3 * n + c] += gbc[(1 + c) * M1 + t];
+    }
     return JLB_OK;
 }
 

@@ -29,6 +29,7 @@ EXPORTED_SYMBOLS = (
     "jlb_last_error", "jlb_batch_create", "jlb_batch_destroy", "jlb_batch_step", "jlb_batch_moments",
     "jlb_batch_populations", "jlb_batch_info", "jlb_batch_domain_fluid", "jlb_batch_last_error",
     "jlb_adj_create", "jlb_adj_destroy", "jlb_adj_forward", "jlb_adj_backward", "jlb_adj_timers", "jlb_adj_last_error",
+    "jlb_adj_create_moving", "jlb_adj_forward_fields", "jlb_adj_backward_fields",
     "jlb_build_info",
 )
 
@@ -124,6 +125,9 @@ def load() -> ctypes.CDLL:
         "jlb_adj_forward": (ctypes.c_int, [vp, ctypes.c_double, dp, dp, ctypes.c_double, ctypes.c_uint32, dp, dp,
                                            dp]),
         "jlb_adj_backward": (ctypes.c_int, [vp, dp, dp, dp]),
+        "jlb_adj_create_moving": (ctypes.c_int, [cfgp, u8p, dp, ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(vp)]),
+        "jlb_adj_forward_fields": (ctypes.c_int, [vp, ctypes.c_double, dp, dp, dp, ctypes.c_uint32, dp, dp, dp]),
+        "jlb_adj_backward_fields": (ctypes.c_int, [vp, dp, dp, dp, dp]),
         "jlb_adj_timers": (ctypes.c_int, [vp, dp]),
         "jlb_adj_last_error": (ctypes.c_char_p, [vp]),
         "jlb_build_info": (ctypes.c_char_p, []),
