@@ -237,6 +237,14 @@ void jlb_batch_destroy(jlb_batch *b);
 /* advances every domain tsteps steps (one launch per step, graph-replayed);
  * moments of the last step are stored */
 int jlb_batch_step(jlb_batch *b, uint32_t tsteps);
+/* Zou-He data of domain d from den (nx,ny,nz) / vel (nx,ny,nz,3) at its
+ * boundary sites, as Solver.evolve re-reads them at every call
+ * (jyulb/isothermal.pyx:476-502, :1398): the fixed faces; Z1 only when
+ * bc[Z1] is FIXED_DEN or bc[1Z] is FIXED_VEL (:500).  When den is given, the
+ * domain's sites also take it as their previous-step density (Ladd's term of
+ * moving solids), as Solver.evolve does.  Solid velocities stay as created.
+ * Either pointer may be NULL (that field keeps its current values). */
+int jlb_batch_set_bc(jlb_batch *b, int32_t d, const double *den, const double *vel);
 /* den (nx,ny,nz) and vel (nx,ny,nz,3) of domain d on its fluid sites */
 int jlb_batch_moments(jlb_batch *b, int32_t d, double *den, double *vel);
 /* post-collision populations of domain d, (19, nx, ny, nz) FP64 */

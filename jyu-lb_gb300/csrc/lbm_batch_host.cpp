@@ -48,6 +48,8 @@ struct jlb_batch {
     uint32_t *d_sp_info = nullptr;
     double *d_sp_lw = nullptr, *d_sp_bc = nullptr;
     float *d_sp_den = nullptr;
+    std::vector<int64_t> h_sp_node;  // [Msp] packed node of each boundary node
+    std::vector<uint32_t> h_sp_info; // [Msp] its link / face bits
     std::string err;
 };
 
@@ -450,6 +452,8 @@ int jlb_batch_create(int32_t scheme, const jlb_domain *doms, int32_t ndom, void 
         if (e1 || e2 || e3 || e4 || e5) { b->err = "domain upload failed"; return bail(JLB_ERR_CUDA); }
     }
     b->Msp = (int)g_node.size();
+    b->h_sp_node = g_node;
+    b->h_sp_info = g_info;
     if (b->Msp > 0) {
         const int M = b->Msp;
         // node-major [t][19] -> [19][M] as the boundary-node path reads them
@@ -495,6 +499,59 @@ int jlb_batch_step(jlb_batch *b, uint32_t tsteps) {
     int r = batch_run(b, tsteps, true);
     if (r) return r;
     b->tot += tsteps;
+    return JLB_OK;
+}
+
+int jlb_batch_set_bc(jlb_batch *b, int32_t d, const double *den, const double *vel) {
+    if (!b || d < 0 || d >= b->ndom) return bfail(b, JLB_ERR_INVALID_ARG, "bad argument");
+    if (!den && !vel) return JLB_OK;
+    const BatchDomain &B = b->dom[d];
+    const int t0 = b->sp_first[d], t1 = b->sp_first[d + 1], Md = t1 - t0, M = b->Msp;
+    // Zou-He data, slot by slot in face order as at creation: the fixed faces
+    // read den / vel at the node; Z1 only when bc[Z1] is FIXED_DEN or bc[1Z]
+    // is FIXED_VEL (jyulb/isothermal.pyx:500), else den 1, vel 0
+    if (Md > 0) {
+        std::vector<double> bcd((size_t)8 * Md, 0.0);
+        std::vector<float> dp(Md, 0.0f);
+        for (int c = 0; c < 8; ++c)
+            BCK(cudaMemcpyAsync(bcd.data() + (size_t)c * Md, b->d_sp_bc + (size_t)c * M + t0, (size_t)Md * 8,
+                                cudaMemcpyDeviceToHost, b->st));
+        BCK(cudaStreamSynchronize(b->st));
+        for (int u = 0; u < Md; ++u) {
+            const int64_t l = b->h_sp_node[t0 + u] - B.off;
+            const uint32_t faces = (b->h_sp_info[t0 + u] >> SP_FACE_SHIFT) & 0x3Fu;
+            int slot = 0;
+            for (int face = 0; face < 6; ++face) {
+                if (!(faces & (1u << face))) continue;
+                bool refresh = B.bc[face] == BC_FIXED_DEN || B.bc[face] == BC_FIXED_VEL;
+                if (face == 5) refresh = B.bc[5] == BC_FIXED_DEN || B.bc[4] == BC_FIXED_VEL;
+                double *row = bcd.data() + (size_t)(4 * slot) * Md + u;
+                if (refresh) {
+                    if (den) row[0] = den[l];
+                    if (vel) for (int c = 0; c < 3; ++c) row[(size_t)(1 + c) * Md] = vel[3 * l + c];
+                }
+                slot = 1;
+            }
+            if (den) dp[u] = (float)(den[l] - 1.0);
+        }
+        for (int c = 0; c < 8; ++c)
+            BCK(cudaMemcpyAsync(b->d_sp_bc + (size_t)c * M + t0, bcd.data() + (size_t)c * Md, (size_t)Md * 8,
+                                cudaMemcpyHostToDevice, b->st));
+        if (den) BCK(cudaMemcpyAsync(b->d_sp_den + t0, dp.data(), (size_t)Md * 4, cudaMemcpyHostToDevice, b->st));
+        BCK(cudaStreamSynchronize(b->st));
+    }
+    // previous-step density of the dense moving-wall nodes
+    if (den) {
+        std::vector<float> dp((size_t)B.n);
+        BCK(cudaMemcpyAsync(dp.data(), b->dprev + B.off, (size_t)B.n * 4, cudaMemcpyDeviceToHost, b->st));
+        std::vector<uint8_t> cl(B.n);
+        BCK(cudaMemcpyAsync(cl.data(), b->ncls + B.off, B.n, cudaMemcpyDeviceToHost, b->st));
+        BCK(cudaStreamSynchronize(b->st));
+        for (int32_t l = 0; l < B.n; ++l)
+            if (cl[l] != BCLS_SOLID) dp[l] = (float)(den[l] - 1.0);
+        BCK(cudaMemcpyAsync(b->dprev + B.off, dp.data(), (size_t)B.n * 4, cudaMemcpyHostToDevice, b->st));
+        BCK(cudaStreamSynchronize(b->st));
+    }
     return JLB_OK;
 }
 

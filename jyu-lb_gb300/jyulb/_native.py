@@ -26,7 +26,7 @@ EXPORTED_SYMBOLS = (
     "jlb_step", "jlb_download_moments", "jlb_get_populations", "jlb_set_populations", "jlb_bc_data",
     "jlb_reduce", "jlb_residual", "jlb_flow_info", "jlb_reduce_moments_noalloc", "jlb_tot_tsteps", "jlb_rlx_prm", "jlb_kernel_launches",
     "jlb_transfer_bytes", "jlb_host_timers",
-    "jlb_last_error", "jlb_batch_create", "jlb_batch_destroy", "jlb_batch_step", "jlb_batch_moments",
+    "jlb_last_error", "jlb_batch_create", "jlb_batch_destroy", "jlb_batch_step", "jlb_batch_moments", "jlb_batch_set_bc",
     "jlb_batch_populations", "jlb_batch_info", "jlb_batch_domain_fluid", "jlb_batch_last_error",
     "jlb_adj_create", "jlb_adj_destroy", "jlb_adj_forward", "jlb_adj_backward", "jlb_adj_timers", "jlb_adj_last_error",
     "jlb_adj_create_moving", "jlb_adj_forward_fields", "jlb_adj_backward_fields",
@@ -116,6 +116,7 @@ def load() -> ctypes.CDLL:
         "jlb_batch_destroy": (None, [vp]),
         "jlb_batch_step": (ctypes.c_int, [vp, ctypes.c_uint32]),
         "jlb_batch_moments": (ctypes.c_int, [vp, ctypes.c_int32, dp, dp]),
+        "jlb_batch_set_bc": (ctypes.c_int, [vp, ctypes.c_int32, dp, dp]),
         "jlb_batch_populations": (ctypes.c_int, [vp, ctypes.c_int32, dp]),
         "jlb_batch_info": (ctypes.c_int, [vp, ctypes.POINTER(ctypes.c_int64)]),
         "jlb_batch_domain_fluid": (ctypes.c_int32, [vp, ctypes.c_int32]),

@@ -88,6 +88,17 @@ class Ensemble:
         self.tot_tsteps += int(tsteps)
         return self.tot_tsteps
 
+    def set_bc(self, d, den=None, vel=None):
+        """Zou-He data of domain d from den (nx,ny,nz) / vel (nx,ny,nz,3) at
+        its boundary sites, as Solver.evolve re-reads them at every call; den
+        also becomes the sites' previous-step density (moving solids' Ladd
+        term).  None keeps that field's current values."""
+        sh = self.domains[d].phase.shape
+        dd = None if den is None else np.ascontiguousarray(den, dtype=np.float64).reshape(sh)
+        vv = None if vel is None else np.ascontiguousarray(vel, dtype=np.float64).reshape(sh + (3,))
+        self._check(self._lib.jlb_batch_set_bc(self._h, d, _native.dptr(dd) if dd is not None else None,
+                                               _native.dptr(vv) if vv is not None else None))
+
     def moments(self, d):
         """(den, vel) of domain d after the last step; solid sites keep the
         domain's input values."""

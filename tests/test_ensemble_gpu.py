@@ -143,3 +143,52 @@ def test_ensemble_boundary_sets_match_single_domains(scheme):
         assert np.abs(den[fl] - np.asarray(s.get_den())[fl]).max() <= 1e-6, d
         f = ens.populations(d)
         assert np.abs(f[:, fl] - s.populations()[:, fl]).max() <= 1e-7, d
+
+
+@pytest.mark.parametrize("scheme", [1, 2])
+def test_ensemble_boundary_data_change_between_calls(scheme):
+    # Zou-He data and the previous-step density re-read between calls, as
+    # Solver.evolve does: the inlet ramps, the outlet density steps, and the
+    # moving top wall next to the Zou-He faces reads the new density
+    from jyulb.ensemble import Domain, Ensemble
+    from jyulb.isothermal import Solver
+
+    cs = _boundary_domains(9)
+    ens = Ensemble([Domain(c["phase"], c["den"], c["vel"], c["kvisc"], c["g"], c["bc"]) for c in cs], scheme)
+    sol = []
+    for c in cs:
+        s = Solver(np.array(c["phase"].shape, dtype=np.int32), scheme, c["kvisc"], np.array(c["g"]),
+                   np.array(c["bc"], dtype=np.int32), precision=1)
+        s.get_phase()[:] = c["phase"]
+        if c["den"] is not None:
+            s.get_den()[:] = c["den"]
+        if c["vel"] is not None:
+            s.get_vel()[:] = c["vel"]
+        s.finalize_init()
+        sol.append(s)
+    for call, n in enumerate((19, 12, 7)):
+        if call > 0:
+            for d, c in enumerate(cs):
+                den, vel = ens.moments(d)
+                fl = c["phase"] != 0
+                if c["bc"][0] == 3:
+                    vel[0, :, :, 0] = np.where(fl[0], 0.02 + 0.005 * call, vel[0, :, :, 0])
+                if c["bc"][1] == 2:
+                    den[-1] = np.where(fl[-1], 1.0 + 0.002 * call, den[-1])
+                ens.set_bc(d, den, vel)
+                s = sol[d]
+                s.get_den()[fl] = den[fl]
+                s.get_vel()[fl] = vel[fl]
+        ens.evolve(n)
+        for s in sol:
+            s.evolve(n)
+    for d, c in enumerate(cs):
+        fl = c["phase"] != 0
+        den, vel = ens.moments(d)
+        s = sol[d]
+        v32 = np.asarray(s.get_vel())
+        vmax = np.abs(v32[fl]).max()
+        assert np.abs(vel[fl] - v32[fl]).max() <= 1e-5 * vmax + 1e-12, d
+        assert np.abs(den[fl] - np.asarray(s.get_den())[fl]).max() <= 1e-6, d
+        f = ens.populations(d)
+        assert np.abs(f[:, fl] - s.populations()[:, fl]).max() <= 1e-7, d
