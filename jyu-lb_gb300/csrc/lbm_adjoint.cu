@@ -420,8 +420,9 @@ __device__ __forceinline__ void adjoint_dense_sites(const AdjArgs &A, int b, typ
             const double *tg = nullptr;
             const bool on_plane = SEED && i == A.plane;
             if (on_plane) tg = A.target + 3 * ((int64_t)j * a.nz + k);
-            adj_finish<C, ST::shifted, SCH, SEED>(sums, lo, (C)a.g[0], (C)a.g[1], (C)a.g[2], (C)a.w_e, (C)a.w_o, pg,
-                                                 on_plane, tg, a.g[0], a.g[1], a.g[2],
+            adj_finish<C, ST::shifted, SCH, SEED>(sums, lo, arg_g<C>(a, 0), arg_g<C>(a, 1),
+                                                 arg_g<C>(a, 2), arg_we<C>(a),
+                                                 arg_wo<C>(a), pg, on_plane, tg, a.g[0], a.g[1], a.g[2],
                                                  [&]<int q>(C v) { lam[rd.template operator()<q>()] = (S)v; });
         }
     }
@@ -455,8 +456,10 @@ __device__ __forceinline__ void adjoint_boundary_sites(const AdjArgs &A, int b, 
         if (on_plane) tg = A.target + 3 * ((int64_t)j * a.nz + k);
         AdjSums<C, ST::shifted, SCH == SCH_REG> sums;
         adj_accumulate(sums, g, lo);
-        adj_finish<C, ST::shifted, SCH, SEED>(sums, lo, (C)a.g[0], (C)a.g[1], (C)a.g[2], (C)a.w_e, (C)a.w_o, pg, on_plane,
-                                             tg, a.g[0], a.g[1], a.g[2], [&]<int q>(C v) { li[q] = v; });
+        adj_finish<C, ST::shifted, SCH, SEED>(sums, lo, arg_g<C>(a, 0), arg_g<C>(a, 1),
+                                             arg_g<C>(a, 2), arg_we<C>(a), arg_wo<C>(a),
+                                             pg, on_plane, tg, a.g[0], a.g[1], a.g[2],
+                                             [&]<int q>(C v) { li[q] = v; });
         C *lam_den = (C *)A.lam_den;
         if (lam_den) {
             // the density this step stored for the next step's moving-wall

@@ -164,7 +164,12 @@ __global__ void __launch_bounds__(128) lbm_batch_special_kernel(const BatchArgs 
     s.write_moments = a.write_moments;
     s.w_e = D.we;
     s.w_o = D.wo;
-    for (int c = 0; c < 3; ++c) s.g[c] = D.g[c];
+    s.w_ef = D.we;
+    s.w_of = D.wo;
+    for (int c = 0; c < 3; ++c) {
+        s.g[c] = D.g[c];
+        s.gf[c] = D.g[c];
+    }
     for (int f = 0; f < 6; ++f) s.bc[f] = D.bc[f];
     special_node<StoreF32, PhysSh<SCH>, PSTEP, false>(s, (int)blockIdx.x);
 }

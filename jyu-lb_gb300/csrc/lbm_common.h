@@ -106,6 +106,9 @@ struct StepArgs {
     const void *acc;      // optional acceleration field, 3 * Np (compute type), SoA
     double g[3];          // uniform gravity
     double w_e, w_o;      // relaxation rates 1/tau (even / odd)
+    float gf[3];          // g, w_e and w_o rounded to float once by the host:
+    float w_ef, w_of;     // the float kernels read these (a per-thread double
+                          // conversion runs on the narrow FP64 pipe)
     int write_moments;
     // dense-node grid
     int bx, by, kblocks;  // block shape and k-blocks per row-block

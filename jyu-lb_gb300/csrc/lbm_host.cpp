@@ -609,6 +609,9 @@ StepArgs make_args(const jlb_solver *s, int write_moments) {
     a.w_e = s->we; a.w_o = s->wo;
     if (s->prec != PREC_FP64 && s->cfg.kernel == JLB_KERNEL_JYULB)
         float_exact_rates(s->cfg.rlx_scheme == JLB_TRT, s->we, s->wo, a.w_e, a.w_o);
+    for (int d = 0; d < 3; ++d) a.gf[d] = (float)a.g[d];
+    a.w_ef = (float)a.w_e;
+    a.w_of = (float)a.w_o;
     a.write_moments = write_moments;
     const int nzr = ((s->nz + 31) / 32) * 32;
     a.bx = nzr >= 128 ? 128 : nzr;

@@ -131,6 +131,16 @@ __device__ __forceinline__ C bulk_collide(C *fv, C ax, C ay, C az, C we, C wo, C
     else return PH::collide(fv, ax, ay, az, we, wo, ux, uy, uz);
 }
 
+// a double kernel parameter in the compute type: float kernels take the
+// host-rounded copy, double kernels the value itself
+template <class C> __device__ __forceinline__ C par(double d, float f) {
+    if constexpr (sizeof(C) == sizeof(float)) return (C)f;
+    else return (C)d;
+}
+template <class C> __device__ __forceinline__ C arg_g(const StepArgs &a, int d) { return par<C>(a.g[d], a.gf[d]); }
+template <class C> __device__ __forceinline__ C arg_we(const StepArgs &a) { return par<C>(a.w_e, a.w_ef); }
+template <class C> __device__ __forceinline__ C arg_wo(const StepArgs &a) { return par<C>(a.w_o, a.w_of); }
+
 // compile-time loop
 template <int I, int N> struct Unroll {
     template <class F> __device__ __forceinline__ static void run(F &&f) {
@@ -227,18 +237,19 @@ __device__ __forceinline__ void dense_node(const StepArgs &a, int b) {
             const C *acc = (const C *)a.acc;
             fx = __ldg(acc + n); fy = __ldg(acc + Np + n); fz = __ldg(acc + 2 * Np + n);
         }
-        rho = PH::collide_fd(fv, (C)a.g[0], (C)a.g[1], (C)a.g[2], fx, fy, fz, (C)a.w_e, (C)a.w_o, ux, uy, uz);
+        rho = PH::collide_fd(fv, arg_g<C>(a, 0), arg_g<C>(a, 1), arg_g<C>(a, 2), fx, fy, fz, arg_we<C>(a),
+                             arg_wo<C>(a), ux, uy, uz);
     } else {
         C ax, ay, az;
         if (ACCF) {
             const C *acc = (const C *)a.acc;
-            ax = (C)a.g[0] + __ldg(acc + n);
-            ay = (C)a.g[1] + __ldg(acc + Np + n);
-            az = (C)a.g[2] + __ldg(acc + 2 * Np + n);
+            ax = arg_g<C>(a, 0) + __ldg(acc + n);
+            ay = arg_g<C>(a, 1) + __ldg(acc + Np + n);
+            az = arg_g<C>(a, 2) + __ldg(acc + 2 * Np + n);
         } else {
-            ax = (C)a.g[0]; ay = (C)a.g[1]; az = (C)a.g[2];
+            ax = arg_g<C>(a, 0); ay = arg_g<C>(a, 1); az = arg_g<C>(a, 2);
         }
-        rho = bulk_collide<ST, PH>(fv, ax, ay, az, (C)a.w_e, (C)a.w_o, ux, uy, uz);
+        rho = bulk_collide<ST, PH>(fv, ax, ay, az, arg_we<C>(a), arg_wo<C>(a), ux, uy, uz);
     }
 
     // scatter: a population heading into a solid is stored back into this
@@ -324,18 +335,19 @@ __device__ __forceinline__ void special_node(const StepArgs &a, int b) {
             const C *acc = (const C *)a.acc;
             fx = __ldg(acc + n); fy = __ldg(acc + Np + n); fz = __ldg(acc + 2 * Np + n);
         }
-        rho = PH::collide_fd(fv, (C)a.g[0], (C)a.g[1], (C)a.g[2], fx, fy, fz, (C)a.w_e, (C)a.w_o, ux, uy, uz);
+        rho = PH::collide_fd(fv, arg_g<C>(a, 0), arg_g<C>(a, 1), arg_g<C>(a, 2), fx, fy, fz, arg_we<C>(a),
+                             arg_wo<C>(a), ux, uy, uz);
     } else {
         C ax, ay, az;
         if (ACCF) {
             const C *acc = (const C *)a.acc;
-            ax = (C)a.g[0] + __ldg(acc + n);
-            ay = (C)a.g[1] + __ldg(acc + Np + n);
-            az = (C)a.g[2] + __ldg(acc + 2 * Np + n);
+            ax = arg_g<C>(a, 0) + __ldg(acc + n);
+            ay = arg_g<C>(a, 1) + __ldg(acc + Np + n);
+            az = arg_g<C>(a, 2) + __ldg(acc + 2 * Np + n);
         } else {
-            ax = (C)a.g[0]; ay = (C)a.g[1]; az = (C)a.g[2];
+            ax = arg_g<C>(a, 0); ay = arg_g<C>(a, 1); az = arg_g<C>(a, 2);
         }
-        rho = PH::collide(fv, ax, ay, az, (C)a.w_e, (C)a.w_o, ux, uy, uz);
+        rho = PH::collide(fv, ax, ay, az, arg_we<C>(a), arg_wo<C>(a), ux, uy, uz);
     }
 
     S *fo = a.fout ? (S *)a.fout : f;
@@ -414,13 +426,13 @@ __device__ __forceinline__ void sparse_node(const StepArgs &a, int b) {
     C ax, ay, az;
     if (ACCF) {
         const C *acc = (const C *)a.acc;
-        ax = (C)a.g[0] + __ldg(acc + n);
-        ay = (C)a.g[1] + __ldg(acc + a.Np + n);
-        az = (C)a.g[2] + __ldg(acc + 2 * a.Np + n);
+        ax = arg_g<C>(a, 0) + __ldg(acc + n);
+        ay = arg_g<C>(a, 1) + __ldg(acc + a.Np + n);
+        az = arg_g<C>(a, 2) + __ldg(acc + 2 * a.Np + n);
     } else {
-        ax = (C)a.g[0]; ay = (C)a.g[1]; az = (C)a.g[2];
+        ax = arg_g<C>(a, 0); ay = arg_g<C>(a, 1); az = arg_g<C>(a, 2);
     }
-    const C rho = bulk_collide<ST, PH>(fv, ax, ay, az, (C)a.w_e, (C)a.w_o, ux, uy, uz);
+    const C rho = bulk_collide<ST, PH>(fv, ax, ay, az, arg_we<C>(a), arg_wo<C>(a), ux, uy, uz);
     Unroll<0, Q>::run([&]<int q>() {
         if (!PSTEP) {
             bulk_st<ST, PH, OPP(q)>(f + ((uint32_t)OPP(q) * Npc + m), fv[q]);

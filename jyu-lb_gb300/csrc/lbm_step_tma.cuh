@@ -193,14 +193,14 @@ __global__ void __launch_bounds__(128, JLB_MIN_BLOCKS_TMA) lbm_step_tma_kernel(c
             C ax, ay, az;
             if (ACCF) {
                 const C *acc = (const C *)a.acc;
-                ax = (C)a.g[0] + __ldg(acc + n);
-                ay = (C)a.g[1] + __ldg(acc + Np + n);
-                az = (C)a.g[2] + __ldg(acc + 2 * Np + n);
+                ax = arg_g<C>(a, 0) + __ldg(acc + n);
+                ay = arg_g<C>(a, 1) + __ldg(acc + Np + n);
+                az = arg_g<C>(a, 2) + __ldg(acc + 2 * Np + n);
             } else {
-                ax = (C)a.g[0]; ay = (C)a.g[1]; az = (C)a.g[2];
+                ax = arg_g<C>(a, 0); ay = arg_g<C>(a, 1); az = arg_g<C>(a, 2);
             }
             C ux, uy, uz;
-            const C rho = bulk_collide<ST, PH>(fv, ax, ay, az, (C)a.w_e, (C)a.w_o, ux, uy, uz);
+            const C rho = bulk_collide<ST, PH>(fv, ax, ay, az, arg_we<C>(a), arg_wo<C>(a), ux, uy, uz);
             Unroll<0, Q>::run([&]<int q>() {
                 if (!PSTEP) {
                     bulk_st<ST, PH, OPP(q)>(f + ((int32_t)OPP(q) * Np + n), fv[q]);
@@ -316,19 +316,19 @@ __global__ void __launch_bounds__(128, JLB_MIN_BLOCKS_H2) lbm_step_tma_h2_kernel
             C axA, ayA, azA, axB, ayB, azB;
             if (ACCF) {
                 const C *acc = (const C *)a.acc;
-                axA = (C)a.g[0] + __ldg(acc + nA); axB = (C)a.g[0] + __ldg(acc + nA + 1);
-                ayA = (C)a.g[1] + __ldg(acc + Np + nA); ayB = (C)a.g[1] + __ldg(acc + Np + nA + 1);
-                azA = (C)a.g[2] + __ldg(acc + 2 * Np + nA); azB = (C)a.g[2] + __ldg(acc + 2 * Np + nA + 1);
+                axA = arg_g<C>(a, 0) + __ldg(acc + nA); axB = arg_g<C>(a, 0) + __ldg(acc + nA + 1);
+                ayA = arg_g<C>(a, 1) + __ldg(acc + Np + nA); ayB = arg_g<C>(a, 1) + __ldg(acc + Np + nA + 1);
+                azA = arg_g<C>(a, 2) + __ldg(acc + 2 * Np + nA); azB = arg_g<C>(a, 2) + __ldg(acc + 2 * Np + nA + 1);
             } else {
-                axA = axB = (C)a.g[0]; ayA = ayB = (C)a.g[1]; azA = azB = (C)a.g[2];
+                axA = axB = arg_g<C>(a, 0); ayA = ayB = arg_g<C>(a, 1); azA = azB = arg_g<C>(a, 2);
             }
             C hA[Q], hB[Q];
             Unroll<0, Q>::run([&]<int q>() { hA[q] = __low2float(*(const __half2 *)&w[q]); });
             C uxA, uyA, uzA;
-            const C rhoA = PH::collide_h(hA, axA, ayA, azA, (C)a.w_e, (C)a.w_o, uxA, uyA, uzA);
+            const C rhoA = PH::collide_h(hA, axA, ayA, azA, arg_we<C>(a), arg_wo<C>(a), uxA, uyA, uzA);
             Unroll<0, Q>::run([&]<int q>() { hB[q] = __high2float(*(const __half2 *)&w[q]); });
             C uxB, uyB, uzB;
-            const C rhoB = PH::collide_h(hB, axB, ayB, azB, (C)a.w_e, (C)a.w_o, uxB, uyB, uzB);
+            const C rhoB = PH::collide_h(hB, axB, ayB, azB, arg_we<C>(a), arg_wo<C>(a), uxB, uyB, uzB);
             // local step: population q of both sites goes to slot opp(q)
             Unroll<0, Q>::run([&]<int q>() {
                 __half *p = f + ((int32_t)OPP(q) * Np + nA);
