@@ -225,3 +225,59 @@ def test_loss_fn_backward_differentiates_its_own_forward_run():
     l2.backward()
     assert abs(float(t2.grad) - 1.8) < 1e-15
     assert p.forwards == 4
+
+
+def test_new_entry_points_reject_null_handles_without_a_gpu():
+    # argument checks come before any CUDA call
+    from jyulb import _native
+
+    lib = _lib()
+    inv = _native.JLB_ERR_INVALID_ARG
+    g = (ctypes.c_double * 3)(0.0, 0.0, 0.0)
+    loss = ctypes.c_double()
+    assert lib.jlb_adj_forward_fields(None, 0.8, g, None, None, 1, None, ctypes.byref(loss), None) == inv
+    assert lib.jlb_adj_backward_fields(None, None, None, None, None) == inv
+    assert lib.jlb_adj_backward(None, None, None, None) == inv
+    h = ctypes.c_void_p()
+    ph = np.ones((4, 4, 4), np.uint8)
+    assert lib.jlb_adj_create_moving(ctypes.byref(_cfg()), _native.u8ptr(ph), None, 1, 5, ctypes.byref(h)) == inv
+    assert b"solid velocity" in lib.jlb_adj_last_error(None)
+    assert lib.jlb_batch_set_bc(None, 0, None, None) == inv
+
+
+def test_field_loss_fn_backward_differentiates_its_own_forward_run():
+    """field_loss_fn follows loss_fn's rule for two graphs on one problem."""
+    torch = pytest.importorskip("torch")
+    from jyulb.adjoint import field_loss_fn
+
+    class FakeProblem:
+        def __init__(self):
+            self.run_id = 0
+            self.last = None
+            self.forwards = 0
+
+        def forward_fields(self, tau, g, den, vel, steps, target=None):
+            self.run_id += 1
+            self.forwards += 1
+            self.last = (tau, den.copy(), vel.copy())
+            return tau * float(den.sum()), None
+
+        def backward_fields(self):
+            tau, den, vel = self.last
+            return float(den.sum()), np.zeros(3), np.full(den.shape, tau), np.zeros(vel.shape)
+
+    p = FakeProblem()
+    g = torch.zeros(3, dtype=torch.float64)
+    d1 = torch.ones(2, 2, 2, dtype=torch.float64, requires_grad=True)
+    d2 = torch.full((2, 2, 2), 2.0, dtype=torch.float64, requires_grad=True)
+    v = torch.zeros(2, 2, 2, 3, dtype=torch.float64)
+    t1 = torch.tensor(0.6, dtype=torch.float64, requires_grad=True)
+    t2 = torch.tensor(0.9, dtype=torch.float64, requires_grad=True)
+    l1 = field_loss_fn(p, t1, g, d1, v, None, 10)
+    l2 = field_loss_fn(p, t2, g, d2, v, None, 10)
+    l1.backward()
+    assert abs(float(t1.grad) - 8.0) < 1e-15 and np.allclose(d1.grad.numpy(), 0.6)
+    assert p.forwards == 3
+    l2.backward()
+    assert abs(float(t2.grad) - 16.0) < 1e-15 and np.allclose(d2.grad.numpy(), 0.9)
+    assert p.forwards == 4
