@@ -21,6 +21,26 @@ namespace jlb {
 #ifndef JLB_BATCH_WARPS
 #define JLB_BATCH_WARPS 32
 #endif
+// lane l of warp 0 prefetches lines l, l + 32, ... of the 19 population rows
+// tile t reads (slot opp(q) at x - c_q in the pull-push step, slot q at x in
+// the local step), clamped to the tile's domain; the periodic wrap is ignored
+template <bool PSTEP, int BLOCK>
+__device__ __forceinline__ void batch_prefetch(const BatchArgs &a, int t, int lane) {
+    const BatchDomain &D = a.dom[__ldg(a.tile_dom + t)];
+    const int32_t l0 = (t - D.first_tile) * BLOCK;
+    const int32_t syz = D.ny * D.nz;
+    constexpr int LPR = BLOCK * (int)sizeof(float) / 128 + 1; // 128-byte lines per row
+#pragma unroll 1
+    for (int idx = lane; idx < Q * LPR; idx += 32) {
+        const int q = idx / LPR, line = idx - q * LPR;
+        const int32_t dq = PSTEP ? CX(q) * syz + CY(q) * D.nz + CZ(q) : 0;
+        int32_t e = l0 - dq - 1 + line * (128 / (int)sizeof(float));
+        if (e < 0) e = 0;
+        if (e >= D.n) continue;
+        prefetch_line(a.fq[PSTEP ? OPP(q) : q] + D.off + e);
+    }
+}
+
 // IDX32: every element index q * Np + n fits 32 unsigned bits (19 Np < 2^32),
 // so an address is one select of two 32-bit indices and one widening
 // multiply-add; otherwise each population row has its own 64-bit pointer
@@ -31,6 +51,7 @@ __global__ void __launch_bounds__(BLOCK, JLB_BATCH_WARPS * 32 / BLOCK)
     using PH = PhysSh<SCH>;
     using C = float;
     const int t = (int)blockIdx.x;
+    if (a.pf && threadIdx.x < 32 && t + a.pf < a.ntiles) batch_prefetch<PSTEP, BLOCK>(a, t + a.pf, (int)threadIdx.x);
     const int d = __ldg(a.tile_dom + t);
     const BatchDomain &D = a.dom[d];
     const int32_t l = (t - D.first_tile) * BLOCK + (int)threadIdx.x;

@@ -38,6 +38,9 @@ struct BatchArgs {
     float *dprev;          // previous-step rho - 1 (MOVING nodes)
     float *den, *ux, *uy, *uz;
     int write_moments;
+    int ntiles;            // tiles of the launch
+    int pf;                // L2 prefetch distance in tiles: the block of tile t
+                           // prefetches the rows tile t + pf reads (0: none)
     // boundary nodes of the domains with Zou-He or symmetric faces, in the
     // single-domain table layout ([19][Msp] element indices into f, Zou-He
     // data fixed at set-up) with the domain of each

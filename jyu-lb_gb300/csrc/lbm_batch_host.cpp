@@ -6,6 +6,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -48,6 +49,10 @@ struct jlb_batch {
     uint32_t *d_sp_info = nullptr;
     double *d_sp_lw = nullptr, *d_sp_bc = nullptr;
     float *d_sp_den = nullptr;
+    int pf = 0;                      // L2 prefetch distance in tiles of the current block size
+    int pf_tiles = -1;               // JLB_BATCH_PF: fixed distance in tiles (0: none)
+    bool pf_big = false;             // populations larger than twice the L2
+    int sms = 0;                     // multiprocessors of the device
     std::vector<int64_t> h_sp_node;  // [Msp] packed node of each boundary node
     std::vector<uint32_t> h_sp_info; // [Msp] its link / face bits
     std::string err;
@@ -82,6 +87,8 @@ BatchArgs batch_args(const jlb_batch *b, int write_moments) {
     a.dprev = b->dprev;
     a.den = b->mom[0]; a.ux = b->mom[1]; a.uy = b->mom[2]; a.uz = b->mom[3];
     a.write_moments = write_moments;
+    a.ntiles = b->ntiles;
+    a.pf = b->pf;
     a.Msp = b->Msp;
     a.sp_dom = b->d_sp_dom;
     a.sp_node = b->d_sp_node; a.sp_rd = b->d_sp_rd; a.sp_wr = b->d_sp_wr;
@@ -101,6 +108,13 @@ int batch_tiles(jlb_batch *b, int block) {
     }
     b->ntiles = (int)td.size();
     b->block = block;
+    // L2 prefetch distance: 3/4 of a wave of resident tiles (the launch
+    // bounds ask for 32 warps per SM, so 1024 / block tiles per SM) where the
+    // populations exceed twice the L2, or JLB_BATCH_PF tiles.  On the
+    // 512-channel ensemble (14.5 GB): 37.2 GLUPS without, 40.6 / 41.1 / 41.0 /
+    // 40.9 / 40.8 at 1/2, 3/4, 1, 5/4, 3/2 of a wave
+    b->pf = b->pf_tiles >= 0 ? b->pf_tiles
+                             : b->pf_big ? (int)std::lround(0.75 * b->sms * (1024.0 / block)) : 0;
     if (b->tile_dom) cudaFree(b->tile_dom);
     b->tile_dom = nullptr;
     BCK(cudaMalloc(&b->tile_dom, td.size() * sizeof(int32_t)));
@@ -485,6 +499,19 @@ int jlb_batch_create(int32_t scheme, const jlb_domain *doms, int32_t ndom, void 
         up(b->d_sp_bc, bcd.data(), bcd.size() * 8);
         up(b->d_sp_den, g_den.data(), (size_t)M * 4);
         if (e != cudaSuccess) { b->err = "boundary-node table upload failed"; return bail(JLB_ERR_CUDA); }
+    }
+    {
+        int dev = 0, l2 = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, dev) != cudaSuccess) {
+            cudaGetLastError();
+            b->sms = 0;
+            l2 = 0;
+        }
+        b->pf_big = 19.0 * (double)b->Np * sizeof(float) > 2.0 * (double)l2;
+        const char *e = std::getenv("JLB_BATCH_PF");
+        if (e && e[0]) b->pf_tiles = std::max(0, std::atoi(e));
     }
     const char *tune = std::getenv("JLB_BATCH_BLOCK");
     if (tune && tune[0]) r = batch_tiles(b, std::atoi(tune));

@@ -192,3 +192,20 @@ def test_ensemble_boundary_data_change_between_calls(scheme):
         assert np.abs(den[fl] - np.asarray(s.get_den())[fl]).max() <= 1e-6, d
         f = ens.populations(d)
         assert np.abs(f[:, fl] - s.populations()[:, fl]).max() <= 1e-7, d
+
+
+@pytest.mark.parametrize("pf", ["3", "40"])
+def test_ensemble_prefetch_changes_nothing(pf, monkeypatch):
+    # the L2 line prefetch (forced here: these domains fit in L2, where it is
+    # off by default) is a hint; results are bit for bit those without it
+    from jyulb.ensemble import Domain, Ensemble
+
+    cs = channels(5, 300)
+    out = []
+    for v in ("0", pf):
+        monkeypatch.setenv("JLB_BATCH_PF", v)
+        ens = Ensemble([Domain(c["phase"], None, c["vel"], c["kvisc"], c["g"]) for c in cs], 1)
+        ens.evolve(23)
+        out.append([ens.populations(d) for d in range(len(cs))])
+    for f0, f1 in zip(*out):
+        np.testing.assert_array_equal(f0, f1)
