@@ -286,17 +286,19 @@ int jlb_adj_backward(jlb_adjoint *a, double *dtau, double dg[3], double *duin);
  * each boundary site's previous-step density. */
 int jlb_adj_create_moving(const jlb_config *cfg, const uint8_t *phase, const double *solid_vel, int32_t loss_plane,
                           int32_t checkpoint_every, jlb_adjoint **out);
-/* Forward run whose Zou-He data come from den (nx,ny,nz) and vel (nx,ny,nz,3)
- * at the boundary sites, as Solver.evolve reads them
- * (jyulb/isothermal.pyx:476-502): every FIXED_VEL and FIXED_DEN face, any of
- * the six; Z1 only when bc[Z1] is FIXED_DEN or bc[1Z] is FIXED_VEL (:500), the
- * others keep den 1, vel 0.  NULL den or vel: 1 or 0 everywhere. */
+/* Forward run from rest whose inputs come from den (nx,ny,nz) and vel
+ * (nx,ny,nz,3) where Solver.evolve reads them at its call: the Zou-He data of
+ * the boundary sites (jyulb/isothermal.pyx:476-502), on every FIXED_VEL and
+ * FIXED_DEN face, any of the six (Z1 only when bc[Z1] is FIXED_DEN or bc[1Z]
+ * is FIXED_VEL, :500; the others keep den 1, vel 0), and the first step's
+ * previous-step density of the sites next to moving solids (Ladd's term).
+ * NULL den or vel: 1 or 0 everywhere. */
 int jlb_adj_forward_fields(jlb_adjoint *a, double tau, const double g[3], const double *den, const double *vel,
                            uint32_t steps, const double *target, double *loss, double *u_plane);
 /* gradients of the last forward run's loss w.r.t. tau, g and the den / vel
- * values its Zou-He faces read (zero elsewhere); dden (nx,ny,nz), dvel
- * (nx,ny,nz,3), either may be NULL.  After jlb_adj_forward, the face-1X
- * u_x entries carry duin and the rest is zero. */
+ * values it read (zero elsewhere); dden (nx,ny,nz), dvel (nx,ny,nz,3), either
+ * may be NULL.  After jlb_adj_forward, the face-1X u_x entries carry duin and
+ * the rest is zero. */
 int jlb_adj_backward_fields(jlb_adjoint *a, double *dtau, double dg[3], double *dden, double *dvel);
 /* device time (ms, CUDA events on the problem's stream) of the last runs:
  * out[0] forward, out[1] recomputation, out[2] reverse sweep, out[3] the

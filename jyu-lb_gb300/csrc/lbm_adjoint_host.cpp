@@ -43,6 +43,7 @@ struct jlb_adjoint {
     int ckpt_spd_cap = 0;         // segments ckpt_spd holds
     void *lam_den = nullptr;      // [M] adjoint of the boundary sites' density
     bool moving = false;          // some boundary site has a moving-wall link
+    bool den_param = false;       // the last forward run took den as a parameter
     uint32_t param_faces = 0;     // faces whose Zou-He data the last forward run took as parameters
     int nparts = 0;           // per-block sensitivity slots
     uint32_t steps = 0;
@@ -192,8 +193,10 @@ int adj_create(const jlb_config *cfg, const uint8_t *phase, const double *solid_
 // Zou-He data of boundary site t on face `face`: out = (den, ux, uy, uz)
 using BcFill = std::function<void(int t, int face, int64_t n, double *out)>;
 
+// den_field (nx,ny,nz) or NULL: the boundary sites' previous-step density
+// for the first step, as Solver.evolve reads it from den; NULL: 1 (rest)
 int adj_forward(jlb_adjoint *A, double tau, const double g[3], const BcFill &fill, uint32_t param_faces,
-                uint32_t steps, const double *target, double *loss, double *u_plane) {
+                const double *den_field, uint32_t steps, const double *target, double *loss, double *u_plane) {
     if (!A || !g || steps < 1) return afail(A, JLB_ERR_INVALID_ARG, "bad argument");
     if (!(tau > 0.5)) return afail(A, JLB_ERR_INVALID_ARG, "tau must exceed 1/2");
     jlb_solver *s = A->s;
@@ -222,7 +225,19 @@ int adj_forward(jlb_adjoint *A, double tau, const double g[3], const BcFill &fil
     const int nseg = (int)((steps + A->K - 1) / A->K);
     if (M > 0) {
         ACK(cudaMemcpyAsync(s->d_sp_bc, bc.data(), nb * sizeof(double), cudaMemcpyHostToDevice, s->st));
-        ACK(cudaMemcpyAsync(s->d_sp_den, A->spd0, (size_t)M * s->csz, cudaMemcpyDeviceToDevice, s->st));
+        if (den_field) {
+            std::vector<double> d64(M);
+            std::vector<float> d32(M);
+            for (int t = 0; t < M; ++t) {
+                d64[t] = den_field[s->sp_node[t]];
+                d32[t] = (float)(d64[t] - 1.0);
+            }
+            ACK(cudaMemcpyAsync(s->d_sp_den, s->prec == PREC_FP64 ? (const void *)d64.data() : (const void *)d32.data(),
+                                (size_t)M * s->csz, cudaMemcpyHostToDevice, s->st));
+            ACK(cudaStreamSynchronize(s->st));
+        } else {
+            ACK(cudaMemcpyAsync(s->d_sp_den, A->spd0, (size_t)M * s->csz, cudaMemcpyDeviceToDevice, s->st));
+        }
         if (A->ckpt_spd_cap < nseg) {
             ACK(cudaStreamSynchronize(s->st));
             if (A->ckpt_spd) cudaFree(A->ckpt_spd);
@@ -233,6 +248,7 @@ int adj_forward(jlb_adjoint *A, double tau, const double g[3], const BcFill &fil
         }
     }
     A->param_faces = param_faces;
+    A->den_param = den_field != nullptr;
     // forward with checkpoints
     ACK(adj_events(A, 2));
     ACK(cudaEventRecord(A->ev[0], s->st));
@@ -410,7 +426,22 @@ int adj_backward(jlb_adjoint *A, double *dtau, double dg[3], std::vector<double>
     ACK(cudaMemcpyAsync(part.data(), A->d_part, part.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
     gbc.assign(4 * M1, 0.0);
     ACK(cudaMemcpyAsync(gbc.data(), A->d_gbc, 4 * sizeof(double) * M1, cudaMemcpyDeviceToHost, st));
+    // the adjoint of the first step's previous-step density is the gradient
+    // of den at the boundary sites, when den was a parameter
+    std::vector<double> lam0;
+    if (A->den_param && A->moving) {
+        lam0.resize(M1);
+        if (s->prec == PREC_FP64) {
+            ACK(cudaMemcpyAsync(lam0.data(), A->lam_den, M1 * sizeof(double), cudaMemcpyDeviceToHost, st));
+        } else {
+            std::vector<float> l32(M1);
+            ACK(cudaMemcpyAsync(l32.data(), A->lam_den, M1 * sizeof(float), cudaMemcpyDeviceToHost, st));
+            ACK(cudaStreamSynchronize(st));
+            for (size_t t = 0; t < M1; ++t) lam0[t] = l32[t];
+        }
+    }
     ACK(cudaStreamSynchronize(st));
+    for (size_t t = 0; t < lam0.size(); ++t) gbc[t] += lam0[t];
     double gr[5] = {0, 0, 0, 0, 0};
     for (int b = 0; b < A->nparts; ++b)
         for (int c = 0; c < 5; ++c) gr[c] += part[5 * (size_t)b + c];
@@ -480,7 +511,7 @@ int jlb_adj_forward(jlb_adjoint *A, double tau, const double g[3], const double 
         }
     };
     const uint32_t pf = s->cfg.bc[0] == JLB_FIXED_VEL ? 1u : 0u;
-    return adj_forward(A, tau, g, fill, pf, steps, target, loss, u_plane);
+    return adj_forward(A, tau, g, fill, pf, nullptr, steps, target, loss, u_plane);
 }
 
 int jlb_adj_forward_fields(jlb_adjoint *A, double tau, const double g[3], const double *den, const double *vel,
@@ -493,7 +524,7 @@ int jlb_adj_forward_fields(jlb_adjoint *A, double tau, const double g[3], const 
         if (den) d[0] = den[n];
         if (vel) for (int c = 0; c < 3; ++c) d[1 + c] = vel[3 * n + c];
     };
-    return adj_forward(A, tau, g, fill, pf, steps, target, loss, u_plane);
+    return adj_forward(A, tau, g, fill, pf, den, steps, target, loss, u_plane);
 }
 
 int jlb_adj_backward(jlb_adjoint *A, double *dtau, double dg[3], double *duin) {

@@ -229,3 +229,53 @@ def test_field_loss_fn_autograd():
     assert float(tau.grad) == pytest.approx(dtau, rel=1e-12)
     np.testing.assert_allclose(v.grad.numpy(), dvel, rtol=1e-12)
     np.testing.assert_allclose(d.grad.numpy(), dden, rtol=1e-12)
+
+
+@pytest.mark.parametrize("kind,scheme", [("y", "TRT"), ("z", "TRT"), ("x1", "REG"), ("lid", "TRT"), ("lid", "REG")])
+def test_fp64_field_adjoint_matches_torch_autograd(kind, scheme):
+    # every entry of d/d den and d/d vel, with tau and g, against autograd
+    # through the pure-torch FP64 step, which the oracle pins on the CPU
+    # (test_general_torch_step_matches_oracle, same cases)
+    import torch
+
+    from jyulb.adjoint import ChannelProblem
+    from jyulb.defs import FP64
+    from pyoracle import Oracle
+    from test_oracle_golden import _field_case
+    from torch_lbm import run_fields
+
+    phase, bc, den, vel, sv = _field_case(kind)
+    nx, ny, nz = phase.shape
+    tau, g, steps, plane = 0.8, np.array([2e-6, -1e-6, 1e-6]), 15, nx // 2 + 1
+    magic = 0.25 if scheme == "TRT" else None
+    sch = {"TRT": 1, "REG": 2}[scheme]
+    rng = np.random.default_rng(8)
+    target = 0.01 * rng.standard_normal((ny, nz, 3))
+    p = ChannelProblem(phase, bc=bc, rlx_scheme=sch, precision=FP64, trt_magic=magic, loss_plane=plane,
+                       checkpoint_every=4, solid_vel=sv)
+    L, _ = p.forward_fields(tau, g, den, vel, steps, target)
+    dtau, dg, dden, dvel = p.backward_fields()
+
+    o = Oracle(list(phase.shape), sch, (tau - 0.5) / 3.0, list(g), bc, magic or 0.0)
+    o.get_phase()[:] = phase
+    if sv is not None:
+        o.get_vel()[:] = sv
+    o.finalize_init()
+    t_tau = torch.tensor(tau, dtype=torch.float64, requires_grad=True)
+    t_g = torch.tensor(g, requires_grad=True)
+    t_den = torch.tensor(den, requires_grad=True)
+    t_vel = torch.tensor(vel, requires_grad=True)
+    u = run_fields(phase, t_tau, t_g, t_den, t_vel, steps, bc, magic=magic, scheme=scheme, solid_vel=sv,
+                   f0=o.populations())
+    fl = torch.from_numpy(phase[plane] != 0)
+    d = u[:, plane].permute(1, 2, 0) - torch.tensor(target)
+    Lt = (d[fl] ** 2).sum()
+    Lt.backward()
+    lt = float(Lt.detach())
+    assert abs(L - lt) <= 1e-10 * abs(lt)
+    assert abs(dtau - float(t_tau.grad)) <= 1e-8 * abs(float(t_tau.grad))
+    np.testing.assert_allclose(dg, t_g.grad.numpy(), rtol=1e-8, atol=1e-10 * np.abs(t_g.grad.numpy()).max())
+    gd, gv = t_den.grad.numpy(), t_vel.grad.numpy()
+    np.testing.assert_allclose(dden, gd, rtol=1e-7, atol=1e-9 * max(np.abs(gd).max(), np.abs(gv).max()))
+    np.testing.assert_allclose(dvel, gv, rtol=1e-7, atol=1e-9 * max(np.abs(gd).max(), np.abs(gv).max()))
+    assert np.abs(gd).max() > 0 and np.abs(gv).max() > 0

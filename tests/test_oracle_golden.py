@@ -133,3 +133,75 @@ def test_oracle_matches_reference_digests_at_1000_steps(name):
     assert digest(o.get_vel()[fl]) == h["vel"]
     assert digest(o.den) == h["den_full"]
     assert digest(o.vel) == h["vel_full"]
+
+
+def _field_case(kind, seed=3):
+    """phase, bc, den, vel, solid velocity of the general torch step's cases"""
+    rng = np.random.default_rng(seed)
+    sv = None
+    if kind == "y":
+        shape, bc = (8, 10, 4), [1, 1, 3, 2, 1, 1]
+    elif kind == "z":
+        shape, bc = (6, 6, 10), [1, 1, 0, 0, 3, 2]
+    elif kind == "x1":
+        shape, bc = (12, 6, 4), [2, 3, 0, 0, 1, 1]
+    else:  # moving lid with an inlet
+        shape, bc = (10, 8, 4), [3, 2, 0, 0, 1, 1]
+    nx, ny, nz = shape
+    phase = np.ones(shape, np.uint8)
+    phase[nx // 2 - 1:nx // 2 + 1, ny // 2 - 1:ny // 2 + 1, :] = 0
+    den = np.ones(shape)
+    vel = np.zeros(shape + (3,))
+    sl = {0: (0, slice(None), slice(None)), 1: (nx - 1, slice(None), slice(None)),
+          2: (slice(None), 0, slice(None)), 3: (slice(None), ny - 1, slice(None)),
+          4: (slice(None), slice(None), 0), 5: (slice(None), slice(None), nz - 1)}
+    for f in range(6):
+        if bc[f] == 3:
+            v = vel[sl[f]]
+            v[..., f >> 1] = (-1 if f & 1 else 1) * (0.02 + 0.004 * rng.standard_normal(v.shape[:-1]))
+            v[..., ((f >> 1) + 1) % 3] = 0.002 * rng.standard_normal(v.shape[:-1])
+            vel[sl[f]] = v
+        elif bc[f] == 2:
+            den[sl[f]] = 1.0 + 0.002 * rng.standard_normal(den[sl[f]].shape)
+            v = vel[sl[f]]
+            v[..., ((f >> 1) + 1) % 3] = 0.001 * rng.standard_normal(v.shape[:-1])
+            vel[sl[f]] = v
+    if kind == "lid":
+        phase[:, -1, :] = 0
+        sv = np.zeros(shape + (3,))
+        sv[:, -1, :, 0] = 0.05
+        sv[:, -1, :, 2] = 0.01
+        den[:, -2, :] += 0.001 * rng.standard_normal((nx, nz))  # read by the lid's Ladd term
+        vel[0, :-1, :, 0] = 0.01 + 0.002 * rng.standard_normal((ny - 1, nz))
+    return phase, bc, den, vel, sv
+
+
+@pytest.mark.parametrize("kind", ["y", "z", "x1", "lid"])
+@pytest.mark.parametrize("scheme", ["TRT", "REG"])
+def test_general_torch_step_matches_oracle(kind, scheme):
+    # the general pure-torch step (Zou-He on any fixed face from den / vel,
+    # moving solids with Ladd's term) reproduces the oracle from rest, with
+    # the face data and the previous-step density read at the evolve call
+    import torch
+
+    from pyoracle import Oracle
+    from torch_lbm import run_fields
+
+    phase, bc, den, vel, sv = _field_case(kind)
+    tau, g, steps = 0.8, np.array([2e-6, -1e-6, 1e-6]), 21
+    sch = {"TRT": 1, "REG": 2}[scheme]
+    o = Oracle(list(phase.shape), sch, (tau - 0.5) / 3.0, list(g), bc, 0.25 if scheme == "TRT" else 0.0)
+    o.get_phase()[:] = phase
+    if sv is not None:
+        o.get_vel()[:] = sv
+    o.finalize_init()
+    f0 = o.populations()  # rest, except next to the moving solids
+    u = run_fields(phase, torch.tensor(tau, dtype=torch.float64), torch.tensor(g), torch.tensor(den),
+                   torch.tensor(vel), steps, bc, magic=0.25 if scheme == "TRT" else None, scheme=scheme,
+                   solid_vel=sv, f0=f0).numpy()
+    fl = phase != 0
+    o.get_den()[fl] = den[fl]
+    o.get_vel()[fl] = vel[fl]
+    o.evolve(steps)
+    ref = np.moveaxis(o.get_vel(), -1, 0)[:, fl]
+    np.testing.assert_allclose(u[:, fl], ref, rtol=0, atol=1e-13 * np.abs(ref).max())
