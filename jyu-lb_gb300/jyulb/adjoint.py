@@ -94,9 +94,11 @@ class ChannelProblem:
         return float(dtau.value), dg, duin
 
     def forward_fields(self, tau, g, den, vel, steps, target=None):
-        """Forward run whose Zou-He faces read den (nx,ny,nz) and vel
-        (nx,ny,nz,3) at their boundary sites (None: 1 and 0); returns (loss,
-        u on the loss plane)."""
+        """Forward run that reads den (nx,ny,nz) and vel (nx,ny,nz,3) where
+        Solver.evolve reads them: the Zou-He data at the boundary sites of the
+        fixed faces, and the first step's previous-step density of the sites
+        next to moving solids (None: 1 and 0); returns (loss, u on the loss
+        plane)."""
         nx, ny, nz = self.shape
         g = np.ascontiguousarray(g, dtype=np.float64).reshape(3)
         d = None if den is None else np.ascontiguousarray(den, dtype=np.float64).reshape(nx, ny, nz)
