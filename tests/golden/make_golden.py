@@ -179,6 +179,27 @@ def large_cases():
     out.append(dict(name="large_channel_reg", lat=list(sh), scheme=REG, kvisc=(0.7 - 0.5) / 3.0,
                     g=[5e-6, 0, 0], bc=[PER, PER, WALL, SYM, PER, PER], phase=ph, den=np.ones(sh),
                     vel=np.zeros(sh + (3,)), acc=None, chunks=[600, 400]))
+    # BGK channel with a Zou-He velocity inlet (profile) on 1X and density
+    # outlet on X1, a solid lid row moving tangentially across both faces
+    # (the corner sites have Zou-He and moving-wall links), seeded obstacles,
+    # a symmetric face on 1Z and a wall on Z1; nz = 36, two evolve calls
+    rng = np.random.default_rng(47)
+    sh = (48, 40, 36)
+    ph = spheres(sh, 3.0, 0.96, rng)
+    ph[:4] = 1
+    ph[-4:] = 1
+    ph[:, -1, :] = 0
+    vel = np.zeros(sh + (3,))
+    vel[:, -1, :, 0] = 0.03
+    vel[:, -1, :, 2] = 0.01
+    y = (np.arange(sh[1]) + 0.5) / (sh[1] - 1)
+    prof = np.clip(4.0 * y * (1.0 - y), 0.0, None)
+    vel[0, :-1, :, 0] = 0.02 * prof[:-1, None]
+    den = np.ones(sh)
+    den[-1] = 0.998
+    out.append(dict(name="large_lid_inlet_bgk", lat=list(sh), scheme=BGK, kvisc=0.04, g=[0, 0, 0],
+                    bc=[FV, FD, WALL, WALL, SYM, WALL], phase=ph, den=den, vel=vel, acc=None,
+                    chunks=[700, 300]))
     return out
 
 

@@ -8,7 +8,12 @@ paths run, against SHA-256 digests of the reference's own arrays
 * large_channel_reg, 64x32x128 regularized channel through spheres (90%
   fluid), gravity, a symmetric face on Y1 (8192 boundary nodes, 64 blocks of
   the boundary-node path): nz = 128 and mostly fluid, so FP32 runs the
-  bulk-copy staged local step.
+  bulk-copy staged local step;
+* large_lid_inlet_bgk, 48x40x36 BGK channel with a Zou-He velocity inlet
+  (profile) and density outlet, a solid lid row moving tangentially across
+  both faces (corner sites with Zou-He and moving-wall links), seeded
+  obstacles, symmetric 1Z and wall Z1, two evolve calls: nz = 36 again takes
+  the consecutive-site blocks.
 
 The FP64 engine must reproduce the reference's populations, den, vel, the
 whole halo-padded den / vel and the twelve bc-data face arrays bit for bit;
