@@ -200,6 +200,23 @@ def large_cases():
     out.append(dict(name="large_lid_inlet_bgk", lat=list(sh), scheme=BGK, kvisc=0.04, g=[0, 0, 0],
                     bc=[FV, FD, WALL, WALL, SYM, WALL], phase=ph, den=den, vel=vel, acc=None,
                     chunks=[700, 300]))
+    # TRT (magic 3/16) flow along z: Zou-He velocity inlet with a profile on
+    # 1Z (Z1 is then read too), density outlet on Z1, periodic x, walls in y,
+    # seeded obstacles, a small body force along z; nz = 64, two evolve calls
+    rng = np.random.default_rng(53)
+    sh = (32, 28, 64)
+    ph = spheres(sh, 2.5, 0.97, rng)
+    ph[:, :, :4] = 1
+    ph[:, :, -4:] = 1
+    vel = np.zeros(sh + (3,))
+    y = (np.arange(sh[1]) + 0.5) / sh[1]
+    vel[:, :, 0, 2] = 0.03 * (4.0 * y * (1.0 - y))[None, :]
+    vel[:, :, 0, 0] = 0.002 * np.sin(2 * np.pi * np.arange(sh[0]) / sh[0])[:, None]
+    den = np.ones(sh)
+    den[:, :, -1] = 1.001
+    out.append(dict(name="large_zflow_trt", lat=list(sh), scheme=TRT, kvisc=0.03, g=[0, 0, 2e-7],
+                    bc=[PER, PER, WALL, WALL, FV, FD], phase=ph, den=den, vel=vel, acc=None,
+                    chunks=[500, 500]))
     return out
 
 

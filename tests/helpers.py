@@ -15,7 +15,7 @@ CASES = ["poiseuille_4x34x4", "cavity_trt", "porous_reg", "pdiff_sym", "couette_
 
 # 1000-step cases on larger lattices: the fixtures hold SHA-256 digests of the
 # reference's arrays (f, den, vel over the fluid sites) instead of the arrays
-LARGE_CASES = ["large_cavity_trt", "large_channel_reg", "large_lid_inlet_bgk"]
+LARGE_CASES = ["large_cavity_trt", "large_channel_reg", "large_lid_inlet_bgk", "large_zflow_trt"]
 
 
 def digest(a) -> str:

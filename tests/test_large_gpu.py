@@ -13,7 +13,10 @@ paths run, against SHA-256 digests of the reference's own arrays
   (profile) and density outlet, a solid lid row moving tangentially across
   both faces (corner sites with Zou-He and moving-wall links), seeded
   obstacles, symmetric 1Z and wall Z1, two evolve calls: nz = 36 again takes
-  the consecutive-site blocks.
+  the consecutive-site blocks;
+* large_zflow_trt, 32x28x64 TRT flow along z from a Zou-He velocity profile
+  on 1Z to a density outlet on Z1, through obstacles, periodic x, walls in y,
+  two evolve calls: the z faces' Zou-He at size.
 
 The FP64 engine must reproduce the reference's populations, den, vel, the
 whole halo-padded den / vel and the twelve bc-data face arrays bit for bit;
